@@ -1,0 +1,334 @@
+"""Benchmark of the fused D3Q19 hot path on GB300.
+
+Workload (one "step" = one fused LBM time step over the whole grid):
+  256 x 128 x 128 cells, sphere r = 0.5 world (D = 32 cells) at the domain
+  centre, Re = 100 (U = 0.05, nu = 0.016, tau = 0.548), MRT collision with the
+  Smagorinsky model (Cs = 0.1), ray-sphere Bouzidi q on a dist^2 <= r^2 mask,
+  Zou-He inlet/outlet, periodic y/z, pre-collision stability guard -- the
+  examples/10_cd_convergence.py step at its 256x128x128 resolution plus
+  Smagorinsky.  Populations stored in FP32 (the headline) and, as extra
+  lines, FP16 / BF16 deviations (f - w).
+
+    python bench.py [--gpus N] [--steps K] [--warmup W] [--impl ours|reference]
+
+Timing: W warm-up steps, then K steps bracketed by barrier + synchronize and
+CUDA events on the launching stream; the A/B state (2 x 319 MB) is larger than
+L2 (129 MB), so every step reads and writes HBM.  With --gpus N > 1 (torchrun)
+each rank runs an independent replica ("replicas only": the path is one
+domain per GPU) and rank 0 prints the aggregate.
+
+The reference arm (--impl reference) times the CPU oracle -- the torch-CPU
+restatement of jax_lbm (JAX itself is not installed) -- on this host's cores.
+"""
+
+import argparse
+import ctypes
+import json
+import os
+import subprocess
+import sys
+import threading
+import time
+
+ROOT = os.path.dirname(os.path.abspath(__file__))
+sys.path.insert(0, ROOT)
+
+NX, NY, NZ = 256, 128, 128
+U = 0.05
+RE = 100.0
+D_CELLS = 2 * 0.5 * NX / 8.0
+NU = U * D_CELLS / RE
+TAU = 3.0 * NU + 0.5
+CS = 0.1
+BYTES_PER_UPDATE = {"fp32": 152, "fp16": 76, "bf16": 76, "fp64": 304}
+WORKLOAD = ("D3Q19 MRT+Smagorinsky(Cs=0.1) sphere D=32 Re=100, Bouzidi ray-sphere q, "
+            "Zou-He in/out, periodic y/z, pre-collision guard, 256x128x128")
+
+
+def _peaks():
+    try:
+        with open(os.path.join(ROOT, "MEASURED_PEAKS.json")) as fh:
+            d = json.load(fh)
+        return float(d["hbm_gbs"]), "measured"
+    except Exception:
+        return 6800.0, "fallback"
+
+
+def _traffic_from_profiles(storage):
+    """Per-launch DRAM bytes of the fused step from the committed ncu summary."""
+    try:
+        with open(os.path.join(ROOT, "profiles", "roofline_traffic.json")) as fh:
+            d = json.load(fh)
+        return d.get(storage)
+    except Exception:
+        return None
+
+
+class ClockSampler:
+    """nvidia-smi clock / throttle sampling during the timed region."""
+
+    FIELDS = ("index,clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.active,"
+              "clocks_event_reasons.hw_slowdown,clocks_event_reasons.hw_thermal_slowdown,"
+              "clocks_event_reasons.sw_thermal_slowdown,clocks_event_reasons.sw_power_cap")
+
+    def __init__(self, index):
+        self.index = index
+        self.proc = None
+        self.lines = []
+
+    def start(self):
+        try:
+            self.proc = subprocess.Popen(
+                ["nvidia-smi", "-i", str(self.index), "--query-gpu=" + self.FIELDS,
+                 "--format=csv,noheader,nounits", "-lms", "100"],
+                stdout=subprocess.PIPE, stderr=subprocess.DEVNULL, text=True)
+            self.t = threading.Thread(target=self._read, daemon=True)
+            self.t.start()
+        except Exception:
+            self.proc = None
+
+    def _read(self):
+        for line in self.proc.stdout:
+            self.lines.append(line.strip())
+
+    def stop(self):
+        if self.proc is None:
+            return None
+        self.proc.terminate()
+        try:
+            self.proc.wait(timeout=5)
+        except Exception:
+            self.proc.kill()
+        sm, mx, reasons = [], None, set()
+        names = ["hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap"]
+        for ln in self.lines:
+            p = [x.strip() for x in ln.split(",")]
+            if len(p) < 9:
+                continue
+            try:
+                sm.append(float(p[1]))
+                mx = float(p[2])
+            except ValueError:
+                continue
+            for nm, v in zip(names, p[5:9]):
+                if v.lower() == "active":
+                    reasons.add(nm)
+        if not sm:
+            return None
+        sm.sort()
+        return {"sm_mhz": sm[len(sm) // 2], "sm_max_mhz": mx, "reasons": sorted(reasons),
+                "samples": len(sm)}
+
+
+def _dist():
+    ws = int(os.environ.get("WORLD_SIZE", "1"))
+    rank = int(os.environ.get("RANK", "0"))
+    local = int(os.environ.get("LOCAL_RANK", "0"))
+    return ws, rank, local
+
+
+def _oracle_step_sample(n_steps, threads):
+    """Time n_steps of the CPU oracle on the bench workload; returns (s, cells*steps)."""
+    import torch
+
+    from oracle import drivers, geometry, ops
+    torch.set_num_threads(threads)
+    solid, q = geometry.create_sphere(NX, NY, NZ, (0.0, 0.0, 0.0), 0.5)
+    f = drivers.initial_state(NX, NY, NZ, U)
+    cfg = drivers.StepConfig(tau=TAU, inlet=(U, 0.0, 0.0), collision="mrt", smagorinsky_cs=CS,
+                             guard="pre")
+    with torch.no_grad():
+        drivers.step(f, q, cfg, solid=solid, f_ref=f)      # warm-up (allocator, threads)
+        t0 = time.perf_counter()
+        g = f
+        for _ in range(n_steps):
+            g, _, _ = drivers.step(g, q, cfg, solid=solid, f_ref=f)
+        dt = time.perf_counter() - t0
+    return dt, NX * NY * NZ * n_steps
+
+
+def run_reference(args):
+    ws, rank, _ = _dist()
+    if rank != 0:
+        return 0
+    threads = os.cpu_count() or 1
+    steps = max(1, args.steps_ref)
+    dt, updates = _oracle_step_sample(steps, threads)
+    mlups = updates / dt / 1e6
+    line = {
+        "impl": "reference",
+        "metric": "fwd MLUPS at 256x128x128 (MRT+Smagorinsky sphere step)",
+        "value": round(mlups, 4), "unit": "MLUPS", "n_gpus": args.gpus,
+        "steps": steps, "warmup": 1, "ms_per_step": round(1e3 * dt / steps, 3),
+        "higher_is_better": True, "scaling": "weak", "vs_baseline": None,
+        "dtype": "f32", "data": "synthetic",
+        "config": {"workload": WORKLOAD, "grid": [NX, NY, NZ]},
+        "cpu_baseline": {"value": round(mlups, 4), "unit": "MLUPS", "cores": threads,
+                         "kind": "port",
+                         "sample": "%d step(s) of the full 256x128x128 workload, torch-CPU "
+                                   "restatement of jax_lbm, %d threads" % (steps, threads)},
+        "e2e": {"value": round(mlups, 4), "unit": "MLUPS", "h2d_bytes_per_step": 0,
+                "d2h_bytes_per_step": 0},
+    }
+    print(json.dumps(line))
+    return 0
+
+
+def _make_sim(storage):
+    from lbm_jax_autodiff_gb300 import Simulation
+    sim = Simulation(NX, NY, NZ, TAU, collision="mrt", storage=storage, use_smagorinsky=True,
+                     smagorinsky_cs=CS, periodic_yz=True, guard="pre",
+                     inlet_velocity=(U, 0.0, 0.0))
+    sim.set_sphere(0.5, center=(0.0, 0.0, 0.0), kind="dist", q_mode="bouzidi", porosity="hard")
+    sim.set_state(sim.equilibrium_state())
+    return sim
+
+
+def _time_steps(sim, steps, warmup, barrier):
+    import torch
+    sim.run(warmup)
+    torch.cuda.synchronize()
+    barrier()
+    st = torch.cuda.current_stream()
+    e0 = torch.cuda.Event(enable_timing=True)
+    e1 = torch.cuda.Event(enable_timing=True)
+    torch.cuda.synchronize()
+    e0.record(st)
+    sim.run(steps)
+    e1.record(st)
+    torch.cuda.synchronize()
+    barrier()
+    return e0.elapsed_time(e1) / 1e3
+
+
+def run_ours(args):
+    import torch
+    ws, rank, local = _dist()
+    torch.cuda.set_device(local)
+    dist = None
+    if ws > 1:
+        import torch.distributed as dist
+        dist.init_process_group("nccl")
+
+    def barrier():
+        if dist is not None:
+            dist.barrier()
+
+    def max_over_ranks(v):
+        if dist is None:
+            return v
+        t = torch.tensor([v], dtype=torch.float64, device="cuda")
+        dist.all_reduce(t, op=dist.ReduceOp.MAX)
+        return float(t.item())
+
+    n_cells = NX * NY * NZ
+    peak, peak_kind = _peaks()
+
+    # headline: FP32 storage
+    sim = _make_sim("fp32")
+    clocks = ClockSampler(local)
+    clocks.start()
+    t = _time_steps(sim, args.steps, args.warmup, barrier)
+    clk = clocks.stop()
+    t = max_over_ranks(t)
+    mlups = ws * n_cells * args.steps / t / 1e6
+    per_launch = t / args.steps
+    achieved = BYTES_PER_UPDATE["fp32"] * n_cells / per_launch / 1e9
+
+    # e2e through the public API with host buffers: chunks of 500 steps, each
+    # H2D of the host state, the steps, D2H of the state and of the sampled Cd
+    chunk = 500
+    n_chunks = max(1, args.steps // chunk)
+    f_host = sim.equilibrium_state().cpu().pin_memory()
+    f_out = torch.empty_like(f_host).pin_memory()
+    cd_host = torch.empty((1, 4), dtype=torch.float64).pin_memory()
+    f_dev = torch.empty_like(f_host, device="cuda")
+    barrier()
+    torch.cuda.synchronize()
+    t0 = time.perf_counter()
+    for _ in range(n_chunks):
+        f_dev.copy_(f_host, non_blocking=True)
+        sim.set_state(f_dev)
+        s = sim.run(chunk, sample_every=chunk)
+        sim.get_state(out=f_dev)
+        f_out.copy_(f_dev, non_blocking=True)
+        cd_host.copy_(s, non_blocking=True)
+        torch.cuda.synchronize()
+    t_e2e = max_over_ranks(time.perf_counter() - t0)
+    e2e_mlups = ws * n_cells * chunk * n_chunks / t_e2e / 1e6
+    state_bytes = 19 * n_cells * 4
+    cd_last = float(cd_host[0, 3])
+    sim.close()
+
+    # secondary lines: 16-bit storage of (f - w)
+    extra = {}
+    for storage in ("fp16", "bf16"):
+        s2 = _make_sim(storage)
+        t2 = max_over_ranks(_time_steps(s2, args.steps, args.warmup, barrier))
+        s2.close()
+        extra[storage] = {
+            "mlups": round(ws * n_cells * args.steps / t2 / 1e6, 1),
+            "achieved_gbs": round(BYTES_PER_UPDATE[storage] * n_cells / (t2 / args.steps) / 1e9, 1),
+            "frac": round(BYTES_PER_UPDATE[storage] * n_cells / (t2 / args.steps) / 1e9 / peak, 4),
+        }
+
+    cpu = None
+    if rank == 0 and ws == 1 and not args.no_cpu_baseline:
+        threads = os.cpu_count() or 1
+        steps_cpu = max(1, args.steps_ref)
+        dt, updates = _oracle_step_sample(steps_cpu, threads)
+        cpu = {"value": round(updates / dt / 1e6, 4), "unit": "MLUPS", "cores": threads,
+               "kind": "port",
+               "sample": "%d step(s) of the full 256x128x128 workload on the torch-CPU "
+                         "restatement of jax_lbm (%d threads)" % (steps_cpu, threads)}
+
+    if rank == 0:
+        line = {
+            "metric": "fwd MLUPS at 256x128x128 (MRT+Smagorinsky sphere step)",
+            "value": round(mlups, 1), "unit": "MLUPS", "n_gpus": ws, "steps": args.steps,
+            "warmup": args.warmup, "ms_per_step": round(1e3 * t / args.steps, 5),
+            "higher_is_better": True, "scaling": "weak", "vs_baseline": None,
+            "dtype": "f32", "data": "synthetic",
+            "config": {"workload": WORKLOAD, "grid": [NX, NY, NZ], "storage": "fp32",
+                       "tau": round(TAU, 6), "l2": "inputs larger than L2 (A/B state 638 MB)",
+                       "parallelism": "replicas" if ws > 1 else "single GPU"},
+            "roofline": {"bound": "hbm", "achieved": round(achieved, 1), "peak": peak,
+                         "unit": "GB/s", "frac": round(achieved / peak, 4),
+                         "peak_kind": peak_kind,
+                         "traffic": _traffic_from_profiles("fp32"),
+                         "algorithmic_bytes_per_update": BYTES_PER_UPDATE["fp32"]},
+            "cpu_baseline": cpu,
+            "e2e": {"value": round(e2e_mlups, 1), "unit": "MLUPS",
+                    "h2d_bytes_per_step": state_bytes // chunk,
+                    "d2h_bytes_per_step": (state_bytes + 32) // chunk,
+                    "note": "public API, host pinned state in/out every %d-step chunk, Cd read back"
+                            % chunk},
+            "gpu_launches": args.steps,
+            "clocks": clk,
+            "storage16": extra,
+            "cd_last_sample": cd_last,
+        }
+        print(json.dumps(line))
+    if dist is not None:
+        dist.destroy_process_group()
+    return 0
+
+
+def main():
+    ap = argparse.ArgumentParser()
+    ap.add_argument("--gpus", type=int, default=1)
+    ap.add_argument("--steps", type=int, default=2000)
+    ap.add_argument("--warmup", type=int, default=20)
+    ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
+    ap.add_argument("--steps-ref", type=int, default=3, help="oracle steps in the CPU sample")
+    ap.add_argument("--no-cpu-baseline", action="store_true")
+    args = ap.parse_args()
+    if args.warmup < 3:
+        args.warmup = 3
+    if args.impl == "reference":
+        return run_reference(args)
+    return run_ours(args)
+
+
+if __name__ == "__main__":
+    sys.exit(main())

@@ -1,0 +1,498 @@
+// C ABI of the fused solver handle (include/lbm_gb300.h).
+#include <cstdio>
+#include <cstring>
+#include <string>
+#include <vector>
+
+#include "../../include/lbm_gb300.h"
+#include "capi_util.cuh"
+#include "sim.cuh"
+
+namespace lbm {
+
+template <class St>
+cudaError_t launch_step(const StepArgs<typename Storage<St>::Re>& a, bool mrt,
+                        cudaStream_t stream);
+cudaError_t launch_force_finalize(const double* part, int nblocks, double dyn_area, double* out,
+                                  cudaStream_t stream);
+
+struct SphereSpec {
+  double c[3];
+  double r;
+  double alpha;
+  int sigmoid_mask;
+  int bouzidi;
+  double disc_floor;
+  double denom_eps;
+};
+template <class Re>
+cudaError_t launch_sphere_fields(const Grid& g, const SphereSpec& s, uint8_t* solid, Re* q,
+                                 Re* dqdr, cudaStream_t st);
+template <class Re>
+cudaError_t launch_q_from_solid(const Grid& g, const uint8_t* solid, double dq, Re* q,
+                                cudaStream_t st);
+cudaError_t launch_solid_from_i32(int n, const int32_t* m, uint8_t* s, cudaStream_t st);
+template <class Re>
+cudaError_t launch_classify(const Grid& g, const uint8_t* solid, const Re* q, const Re* dqdr,
+                            uint32_t* tag, LinkRec* rec, int cap, int* counter, int count_only,
+                            cudaStream_t st);
+cudaError_t launch_area_cols(const Grid& g, const uint8_t* solid, int* col, cudaStream_t st);
+
+}  // namespace lbm
+
+using namespace lbm;
+
+struct lbm_sim {
+  lbm_params p;
+  Grid g;
+  size_t n = 0;
+  size_t st_bytes = 0;       // bytes per stored population value
+  size_t re_bytes = 0;       // bytes per compute value
+  void* S[2] = {nullptr, nullptr};
+  int cur = 0;
+  int state_is_S = 0;        // 0: f_k in fbuf; 1: S_{k-1} in S[cur]
+  long long steps = 0;
+  void* fbuf = nullptr;      // reference-layout f (compute dtype)
+  uint32_t* tag = nullptr;
+  LinkRec* rec = nullptr;
+  int nrec = 0;
+  int nlinks = 0;
+  double area = 0.0;
+  int have_geometry = 0;
+  int porosity_mode = LBM_POROSITY_NONE;
+  int sphere_porosity = 0;   // analytic sigmoid porosity in-kernel
+  lbm_sphere sphere{};
+  void* porosity = nullptr;  // porosity field (compute dtype)
+  void* u_face = nullptr;    // inlet profile (compute dtype)
+  double* partials = nullptr;
+  int nblocks = 0;
+  unsigned long long* guard_count = nullptr;
+};
+
+namespace {
+
+bool is_fp64(const lbm_sim* s) { return s->p.storage == LBM_F64; }
+
+template <class Re>
+void fill_consts(const lbm_params& p, Consts<Re>& K) {
+  const double w[Q] = {1.0 / 3.0,  1.0 / 18.0, 1.0 / 18.0, 1.0 / 18.0, 1.0 / 18.0,
+                       1.0 / 18.0, 1.0 / 18.0, 1.0 / 36.0, 1.0 / 36.0, 1.0 / 36.0,
+                       1.0 / 36.0, 1.0 / 36.0, 1.0 / 36.0, 1.0 / 36.0, 1.0 / 36.0,
+                       1.0 / 36.0, 1.0 / 36.0, 1.0 / 36.0, 1.0 / 36.0};
+  // MRT_RELAXATION_RATES of lattice.py:106-126 (stress slots filled at run time)
+  const double r[Q] = {0.0, 1.19, 1.4, 0.0, 1.2, 0.0, 1.2, 0.0, 1.2, 0.0,
+                       1.4, 0.0,  1.4, 0.0, 0.0, 0.0, 1.98, 1.98, 1.98};
+  for (int i = 0; i < Q; ++i) {
+    K.w[i] = p.exact_constants ? Re(w[i]) : Re(double(float(w[i])));
+    K.rate[i] = p.exact_constants ? Re(r[i]) : Re(double(float(r[i])));
+  }
+}
+
+template <class Re>
+void fill_args(const lbm_sim* s, StepArgs<Re>& a) {
+  memset(&a, 0, sizeof(a));
+  a.tag = s->tag;
+  a.rec = s->rec;
+  a.g = s->g;
+  fill_consts<Re>(s->p, a.K);
+  a.tau = Re(s->p.tau);
+  a.c18cs2 = Re(18.0 * (s->p.smagorinsky_cs * s->p.smagorinsky_cs));
+  int fl = 0;
+  if (s->p.use_smagorinsky) fl |= SF_SMAG;
+  if (s->porosity_mode == LBM_POROSITY_HARD) fl |= SF_SOLID_HARD;
+  if (s->porosity_mode == LBM_POROSITY_SOFT) fl |= s->sphere_porosity ? SF_SOLID_SPHERE : SF_SOLID_FIELD;
+  if (s->p.guard == LBM_GUARD_PRE) fl |= SF_GUARD_PRE;
+  if (s->p.guard == LBM_GUARD_POST) fl |= SF_GUARD_POST;
+  if (s->u_face) fl |= SF_INLET_FACE;
+  a.flags = fl;
+  for (int k = 0; k < 3; ++k) a.u_in[k] = Re(s->p.inlet_velocity[k]);
+  a.u_face = static_cast<const Re*>(s->u_face);
+  a.rho_out = Re(s->p.rho_out);
+  a.sph.c[0] = Re(s->sphere.center[0]);
+  a.sph.c[1] = Re(s->sphere.center[1]);
+  a.sph.c[2] = Re(s->sphere.center[2]);
+  a.sph.r = Re(s->sphere.radius);
+  a.sph.alpha = Re(s->sphere.sharpness);
+  a.sph.sx = Re(s->g.nx / 8.0);
+  a.sph.sy = Re(s->g.ny / 4.0);
+  a.sph.sz = Re(s->g.nz / 4.0);
+  a.porosity = static_cast<const Re*>(s->porosity);
+  // guard reset targets: pre -> f_eq(1, (U,0,0)) (examples/10:160), post -> f_eq(1, 0) = w
+  for (int i = 0; i < Q; ++i) {
+    if (s->p.guard == LBM_GUARD_PRE) {
+      const double U = s->p.inlet_velocity[0];
+      const double eu = ex(i) * U;
+      a.guard_reset[i] = Re(double(a.K.w[i]) * (1.0 + 3.0 * eu + 4.5 * eu * eu - 1.5 * U * U));
+    } else {
+      a.guard_reset[i] = a.K.w[i];
+    }
+  }
+  a.force_partials = s->partials;
+  a.guard_count = s->guard_count;
+}
+
+int launch(const lbm_sim* s, const void* src, void* dst, int extra_flags, cudaStream_t st) {
+  cudaError_t e;
+  const bool mrt = s->p.collision == LBM_MRT;
+  if (is_fp64(s)) {
+    StepArgs<double> a;
+    fill_args<double>(s, a);
+    a.src = src;
+    a.dst = dst;
+    a.flags |= extra_flags;
+    e = launch_step<double>(a, mrt, st);
+  } else {
+    StepArgs<float> a;
+    fill_args<float>(s, a);
+    a.src = src;
+    a.dst = dst;
+    a.flags |= extra_flags;
+    switch (s->p.storage) {
+      case LBM_F32: e = launch_step<float>(a, mrt, st); break;
+      case LBM_F16: e = launch_step<__half>(a, mrt, st); break;
+      default: e = launch_step<__nv_bfloat16>(a, mrt, st); break;
+    }
+  }
+  return cuda_check(e, "k_step launch");
+}
+
+double dyn_area(const lbm_sim* s) {
+  const double U = s->p.u_ref;
+  const double A = s->area > s->p.area_min ? s->area : s->p.area_min;
+  return 0.5 * 1.0 * U * U * A;
+}
+
+void free_geometry(lbm_sim* s) {
+  cudaFree(s->tag);
+  cudaFree(s->rec);
+  cudaFree(s->porosity);
+  s->tag = nullptr;
+  s->rec = nullptr;
+  s->porosity = nullptr;
+  s->nrec = 0;
+  s->nlinks = 0;
+  s->have_geometry = 0;
+}
+
+// Shared tail of the two geometry entry points: classify cells from the dense
+// q (compute dtype), count links, projected area.
+template <class Re>
+int finish_geometry(lbm_sim* s, const uint8_t* solid, const Re* q, const Re* dqdr,
+                    cudaStream_t st) {
+  int* counter = nullptr;
+  int* cols = nullptr;
+  const int ncol = s->g.ny * s->g.nz;
+  LBM_TRY(dev_alloc((void**)&counter, sizeof(int)));
+  if (!s->tag) LBM_TRY(dev_alloc((void**)&s->tag, s->n * sizeof(uint32_t)));
+  int rc = LBM_OK;
+  do {
+    if ((rc = cuda_check(cudaMemsetAsync(counter, 0, sizeof(int), st), "memset"))) break;
+    if ((rc = cuda_check(launch_classify<Re>(s->g, solid, q, dqdr, s->tag, nullptr, 0, counter, 1, st),
+                         "classify count")))
+      break;
+    int count = 0;
+    if ((rc = cuda_check(cudaMemcpyAsync(&count, counter, sizeof(int), cudaMemcpyDeviceToHost, st),
+                         "count D2H")))
+      break;
+    if ((rc = cuda_check(cudaStreamSynchronize(st), "sync"))) break;
+    cudaFree(s->rec);
+    s->rec = nullptr;
+    if (count > 0 && (rc = dev_alloc((void**)&s->rec, size_t(count) * sizeof(LinkRec)))) break;
+    if ((rc = cuda_check(cudaMemsetAsync(counter, 0, sizeof(int), st), "memset"))) break;
+    if ((rc = cuda_check(launch_classify<Re>(s->g, solid, q, dqdr, s->tag, s->rec, count, counter, 0, st),
+                         "classify fill")))
+      break;
+    s->nrec = count;
+    // link count and projected area
+    if ((rc = dev_alloc((void**)&cols, ncol * sizeof(int)))) break;
+    if ((rc = cuda_check(cudaMemsetAsync(cols, 0, ncol * sizeof(int), st), "memset"))) break;
+    if ((rc = cuda_check(launch_area_cols(s->g, solid, cols, st), "area"))) break;
+    std::vector<int> hc(ncol);
+    if ((rc = cuda_check(cudaMemcpyAsync(hc.data(), cols, ncol * sizeof(int), cudaMemcpyDeviceToHost, st),
+                         "area D2H")))
+      break;
+    std::vector<LinkRec> hr(count);
+    if (count > 0 &&
+        (rc = cuda_check(cudaMemcpyAsync(hr.data(), s->rec, count * sizeof(LinkRec),
+                                         cudaMemcpyDeviceToHost, st),
+                         "rec D2H")))
+      break;
+    if ((rc = cuda_check(cudaStreamSynchronize(st), "sync"))) break;
+    long long a = 0;
+    for (int v : hc) a += v;
+    s->area = double(a);
+    int nl = 0;
+    for (const auto& r : hr) nl += __builtin_popcount(r.linkmask);
+    s->nlinks = nl;
+    s->have_geometry = 1;
+  } while (0);
+  cudaFree(counter);
+  cudaFree(cols);
+  return rc;
+}
+
+template <class Re>
+int set_sphere_impl(lbm_sim* s, const lbm_sphere* sp, cudaStream_t st) {
+  uint8_t* solid = nullptr;
+  Re* q = nullptr;
+  Re* dq = nullptr;
+  int rc = LBM_OK;
+  do {
+    if ((rc = dev_alloc((void**)&solid, s->n))) break;
+    if ((rc = dev_alloc((void**)&q, s->n * Q * sizeof(Re)))) break;
+    if ((rc = dev_alloc((void**)&dq, s->n * Q * sizeof(Re)))) break;
+    SphereSpec spec;
+    for (int k = 0; k < 3; ++k) spec.c[k] = sp->center[k];
+    spec.r = sp->radius;
+    spec.alpha = sp->sharpness;
+    spec.sigmoid_mask = sp->kind == LBM_SPHERE_SIGMOID_MASK;
+    spec.bouzidi = sp->q_mode == LBM_Q_BOUZIDI;
+    spec.disc_floor = sp->disc_floor;
+    spec.denom_eps = sp->denom_eps;
+    if ((rc = cuda_check(launch_sphere_fields<Re>(s->g, spec, solid, q, dq, st), "sphere fields")))
+      break;
+    rc = finish_geometry<Re>(s, solid, q, dq, st);
+  } while (0);
+  cudaStreamSynchronize(st);
+  cudaFree(solid);
+  cudaFree(q);
+  cudaFree(dq);
+  return rc;
+}
+
+template <class Re>
+int set_mask_impl(lbm_sim* s, const int32_t* solid_i32, const void* q_user, double default_q,
+                  cudaStream_t st) {
+  uint8_t* solid = nullptr;
+  Re* q = nullptr;
+  int rc = LBM_OK;
+  do {
+    if ((rc = dev_alloc((void**)&solid, s->n))) break;
+    if ((rc = cuda_check(launch_solid_from_i32(int(s->n), solid_i32, solid, st), "solid"))) break;
+    const Re* qq = static_cast<const Re*>(q_user);
+    if (!qq) {
+      if ((rc = dev_alloc((void**)&q, s->n * Q * sizeof(Re)))) break;
+      if ((rc = cuda_check(launch_q_from_solid<Re>(s->g, solid, default_q, q, st), "q from solid")))
+        break;
+      qq = q;
+    }
+    rc = finish_geometry<Re>(s, solid, qq, nullptr, st);
+  } while (0);
+  cudaStreamSynchronize(st);
+  cudaFree(solid);
+  cudaFree(q);
+  return rc;
+}
+
+}  // namespace
+
+extern "C" {
+
+int lbm_api_version(void) { return LBM_GB300_API_VERSION; }
+
+int lbm_create(const lbm_params* p, lbm_sim** out) {
+  if (!p || !out) return set_error(LBM_ERR_ARG, "lbm_create: null argument");
+  *out = nullptr;
+  if (p->nx < 3 || p->ny < 1 || p->nz < 1)
+    return set_error(LBM_ERR_ARG, "lbm_create: need nx >= 3, ny >= 1, nz >= 1");
+  const long long n = (long long)p->nx * p->ny * p->nz;
+  if (n * Q >= (1LL << 31))
+    return set_error(LBM_ERR_UNSUPPORTED, "lbm_create: 19*cells must be < 2^31");
+  if (p->storage < LBM_F32 || p->storage > LBM_BF16)
+    return set_error(LBM_ERR_ARG, "lbm_create: bad storage dtype");
+  if (p->collision != LBM_BGK && p->collision != LBM_MRT)
+    return set_error(LBM_ERR_ARG, "lbm_create: bad collision");
+  if (p->guard < LBM_GUARD_OFF || p->guard > LBM_GUARD_POST)
+    return set_error(LBM_ERR_ARG, "lbm_create: bad guard mode");
+  if (!(p->tau > 0.5)) return set_error(LBM_ERR_ARG, "lbm_create: tau must be > 0.5");
+  if (p->rho_out <= 0.0) return set_error(LBM_ERR_ARG, "lbm_create: rho_out must be > 0");
+  lbm_sim* s = new (std::nothrow) lbm_sim();
+  if (!s) return set_error(LBM_ERR_NOMEM, "lbm_create: host allocation failed");
+  s->p = *p;
+  s->g = Grid{p->nx, p->ny, p->nz, int(n), p->periodic_yz ? 1 : 0};
+  s->n = size_t(n);
+  s->st_bytes = p->storage == LBM_F64 ? 8 : (p->storage == LBM_F32 ? 4 : 2);
+  s->re_bytes = p->storage == LBM_F64 ? 8 : 4;
+  s->nblocks = int((n + 255) / 256);
+  int rc = LBM_OK;
+  do {
+    if ((rc = dev_alloc(&s->S[0], s->n * Q * s->st_bytes))) break;
+    if ((rc = dev_alloc(&s->S[1], s->n * Q * s->st_bytes))) break;
+    if ((rc = dev_alloc(&s->fbuf, s->n * Q * s->re_bytes))) break;
+    if ((rc = dev_alloc((void**)&s->partials, size_t(s->nblocks) * 3 * sizeof(double)))) break;
+    if ((rc = dev_alloc((void**)&s->guard_count, sizeof(unsigned long long)))) break;
+    if ((rc = cuda_check(cudaMemset(s->guard_count, 0, sizeof(unsigned long long)), "memset"))) break;
+    if ((rc = dev_alloc((void**)&s->tag, s->n * sizeof(uint32_t)))) break;
+    if ((rc = cuda_check(cudaMemset(s->tag, 0, s->n * sizeof(uint32_t)), "memset"))) break;
+  } while (0);
+  if (rc) {
+    lbm_destroy(s);
+    return rc;
+  }
+  *out = s;
+  return LBM_OK;
+}
+
+int lbm_destroy(lbm_sim* s) {
+  if (!s) return LBM_OK;
+  cudaFree(s->S[0]);
+  cudaFree(s->S[1]);
+  cudaFree(s->fbuf);
+  cudaFree(s->partials);
+  cudaFree(s->guard_count);
+  cudaFree(s->u_face);
+  free_geometry(s);
+  delete s;
+  return LBM_OK;
+}
+
+int lbm_set_geometry_sphere(lbm_sim* s, const lbm_sphere* sp, void* stream) {
+  if (!s || !sp) return set_error(LBM_ERR_ARG, "lbm_set_geometry_sphere: null argument");
+  if (!(sp->radius > 0.0)) return set_error(LBM_ERR_ARG, "lbm_set_geometry_sphere: radius <= 0");
+  if (sp->porosity < LBM_POROSITY_NONE || sp->porosity > LBM_POROSITY_SOFT ||
+      (sp->q_mode != LBM_Q_HALFWAY && sp->q_mode != LBM_Q_BOUZIDI) ||
+      (sp->kind != LBM_SPHERE_DIST_MASK && sp->kind != LBM_SPHERE_SIGMOID_MASK))
+    return set_error(LBM_ERR_ARG, "lbm_set_geometry_sphere: bad enum");
+  cudaStream_t st = static_cast<cudaStream_t>(stream);
+  cudaFree(s->porosity);
+  s->porosity = nullptr;
+  s->sphere = *sp;
+  s->porosity_mode = sp->porosity;
+  s->sphere_porosity = sp->porosity == LBM_POROSITY_SOFT;
+  return is_fp64(s) ? set_sphere_impl<double>(s, sp, st) : set_sphere_impl<float>(s, sp, st);
+}
+
+int lbm_set_geometry_mask(lbm_sim* s, const int32_t* solid, const void* q, double default_q,
+                          const void* porosity, void* stream) {
+  if (!s || !solid) return set_error(LBM_ERR_ARG, "lbm_set_geometry_mask: null argument");
+  LBM_TRY(check_align(solid, 4, "solid"));
+  LBM_TRY(check_align(q, s->re_bytes, "q"));
+  LBM_TRY(check_align(porosity, s->re_bytes, "porosity"));
+  cudaStream_t st = static_cast<cudaStream_t>(stream);
+  cudaFree(s->porosity);
+  s->porosity = nullptr;
+  s->sphere_porosity = 0;
+  if (porosity) {
+    LBM_TRY(dev_alloc(&s->porosity, s->n * s->re_bytes));
+    LBM_TRY(cuda_check(cudaMemcpyAsync(s->porosity, porosity, s->n * s->re_bytes,
+                                       cudaMemcpyDeviceToDevice, st),
+                       "porosity copy"));
+    s->porosity_mode = LBM_POROSITY_SOFT;
+  } else {
+    s->porosity_mode = LBM_POROSITY_HARD;
+  }
+  return is_fp64(s) ? set_mask_impl<double>(s, solid, q, default_q, st)
+                    : set_mask_impl<float>(s, solid, q, default_q, st);
+}
+
+int lbm_set_inlet_profile(lbm_sim* s, const void* u_face, void* stream) {
+  if (!s) return set_error(LBM_ERR_ARG, "lbm_set_inlet_profile: null handle");
+  cudaStream_t st = static_cast<cudaStream_t>(stream);
+  if (!u_face) {
+    cudaFree(s->u_face);
+    s->u_face = nullptr;
+    return LBM_OK;
+  }
+  LBM_TRY(check_align(u_face, s->re_bytes, "u_face"));
+  const size_t bytes = size_t(3) * s->g.ny * s->g.nz * s->re_bytes;
+  if (!s->u_face) LBM_TRY(dev_alloc(&s->u_face, bytes));
+  return cuda_check(cudaMemcpyAsync(s->u_face, u_face, bytes, cudaMemcpyDeviceToDevice, st),
+                    "inlet copy");
+}
+
+int lbm_set_state(lbm_sim* s, const void* f, void* stream) {
+  if (!s || !f) return set_error(LBM_ERR_ARG, "lbm_set_state: null argument");
+  LBM_TRY(check_align(f, s->re_bytes, "f"));
+  cudaStream_t st = static_cast<cudaStream_t>(stream);
+  LBM_TRY(cuda_check(cudaMemcpyAsync(s->fbuf, f, s->n * Q * s->re_bytes, cudaMemcpyDeviceToDevice, st),
+                     "state copy"));
+  s->state_is_S = 0;
+  s->steps = 0;
+  return LBM_OK;
+}
+
+int lbm_get_state(lbm_sim* s, void* f, void* stream) {
+  if (!s || !f) return set_error(LBM_ERR_ARG, "lbm_get_state: null argument");
+  LBM_TRY(check_align(f, s->re_bytes, "f"));
+  cudaStream_t st = static_cast<cudaStream_t>(stream);
+  if (!s->state_is_S)
+    return cuda_check(cudaMemcpyAsync(f, s->fbuf, s->n * Q * s->re_bytes, cudaMemcpyDeviceToDevice, st),
+                      "state copy");
+  if (!s->have_geometry) return set_error(LBM_ERR_STATE, "lbm_get_state: no geometry");
+  return launch(s, s->S[s->cur], f, SF_STREAM_ONLY, st);
+}
+
+int lbm_run(lbm_sim* s, int n_steps, int sample_every, double* samples, void* stream) {
+  if (!s) return set_error(LBM_ERR_ARG, "lbm_run: null handle");
+  if (n_steps < 0) return set_error(LBM_ERR_ARG, "lbm_run: n_steps < 0");
+  if (sample_every < 0 || (sample_every > 0 && !samples))
+    return set_error(LBM_ERR_ARG, "lbm_run: sample_every > 0 needs a samples buffer");
+  LBM_TRY(check_align(samples, 8, "samples"));
+  if (!s->have_geometry) return set_error(LBM_ERR_STATE, "lbm_run: set a geometry first");
+  cudaStream_t st = static_cast<cudaStream_t>(stream);
+  const double da = dyn_area(s);
+  // force after global step k is computed by the launch that reads S_{k-1}
+  auto want_sample = [&](long long k_global, long long k0) -> long long {
+    if (sample_every <= 0) return -1;
+    const long long rel = k_global - k0;
+    if (rel <= 0 || rel % sample_every) return -1;
+    return rel / sample_every - 1;
+  };
+  const long long k0 = s->steps;
+  for (int L = 1; L <= n_steps; ++L) {
+    if (!s->state_is_S) {
+      LBM_TRY(launch(s, s->fbuf, s->S[s->cur], SF_COLLIDE_ONLY, st));
+      s->state_is_S = 1;
+    } else {
+      const long long kdone = s->steps;  // this launch computes f_{kdone}
+      const long long si = want_sample(kdone, k0);
+      const int extra = si >= 0 ? SF_FORCE : 0;
+      LBM_TRY(launch(s, s->S[s->cur], s->S[1 - s->cur], extra, st));
+      if (si >= 0)
+        LBM_TRY(cuda_check(launch_force_finalize(s->partials, s->nblocks, da, samples + 4 * si, st),
+                           "force finalize"));
+      s->cur = 1 - s->cur;
+    }
+    s->steps += 1;
+  }
+  const long long si = want_sample(s->steps, k0);
+  if (si >= 0) {
+    // sample after the last step: stream-only pass with the force, state unchanged
+    LBM_TRY(launch(s, s->S[s->cur], s->fbuf, SF_STREAM_ONLY | SF_FORCE, st));
+    LBM_TRY(cuda_check(launch_force_finalize(s->partials, s->nblocks, da, samples + 4 * si, st),
+                       "force finalize"));
+  }
+  return LBM_OK;
+}
+
+int lbm_get_projected_area(lbm_sim* s, double* area_host) {
+  if (!s || !area_host) return set_error(LBM_ERR_ARG, "lbm_get_projected_area: null argument");
+  if (!s->have_geometry) return set_error(LBM_ERR_STATE, "lbm_get_projected_area: no geometry");
+  *area_host = s->area;
+  return LBM_OK;
+}
+
+int lbm_get_link_count(lbm_sim* s, int* links_host, int* special_host) {
+  if (!s || !links_host || !special_host)
+    return set_error(LBM_ERR_ARG, "lbm_get_link_count: null argument");
+  *links_host = s->nlinks;
+  *special_host = s->nrec;
+  return LBM_OK;
+}
+
+int lbm_get_guard_resets(lbm_sim* s, unsigned long long* count_host, void* stream) {
+  if (!s || !count_host) return set_error(LBM_ERR_ARG, "lbm_get_guard_resets: null argument");
+  cudaStream_t st = static_cast<cudaStream_t>(stream);
+  LBM_TRY(cuda_check(cudaMemcpyAsync(count_host, s->guard_count, sizeof(unsigned long long),
+                                     cudaMemcpyDeviceToHost, st),
+                     "guard D2H"));
+  return cuda_check(cudaStreamSynchronize(st), "sync");
+}
+
+int lbm_get_steps(lbm_sim* s, long long* steps_host) {
+  if (!s || !steps_host) return set_error(LBM_ERR_ARG, "lbm_get_steps: null argument");
+  *steps_host = s->steps;
+  return LBM_OK;
+}
+
+}  // extern "C"

@@ -1,0 +1,576 @@
+// D3Q19 lattice, population storage and per-cell collision math for sm_103a.
+//
+// Everything here is per-cell register arithmetic shared by the fused step
+// kernels, the adjoint kernels and the per-op drop-in kernels.
+//
+// Reference semantics (jax_lbm):
+//   velocities / opposite / cs^2         core/lattice.py:29-82
+//   MRT moment basis, norms, rates       core/lattice.py:88-391
+//   equilibrium                          core/equilibrium.py:90-151
+//   bgk, mrt, smagorinsky_tau            core/collision.py:46-270
+// The hand-derived vector-Jacobian products (``*_vjp``) are the transposes of
+// those maps; they replace what jax.grad derives through the same code.
+#pragma once
+
+#include <cmath>
+#include <cstdint>
+#include <cuda_bf16.h>
+#include <cuda_fp16.h>
+#include <cuda_runtime.h>
+
+namespace lbm {
+
+constexpr int Q = 19;
+
+__host__ __device__ constexpr int ex(int i) {
+  constexpr int t[19] = {0, 1, -1, 0, 0, 0, 0, 1, -1, 1, -1, 1, -1, 1, -1, 0, 0, 0, 0};
+  return t[i];
+}
+__host__ __device__ constexpr int ey(int i) {
+  constexpr int t[19] = {0, 0, 0, 1, -1, 0, 0, 1, 1, -1, -1, 0, 0, 0, 0, 1, -1, 1, -1};
+  return t[i];
+}
+__host__ __device__ constexpr int ez(int i) {
+  constexpr int t[19] = {0, 0, 0, 0, 0, 1, -1, 0, 0, 0, 0, 1, 1, -1, -1, 1, 1, -1, -1};
+  return t[i];
+}
+__host__ __device__ constexpr int opp(int i) {
+  constexpr int t[19] = {0, 2, 1, 4, 3, 6, 5, 10, 9, 8, 7, 14, 13, 12, 11, 18, 17, 16, 15};
+  return t[i];
+}
+
+// Moment matrix row k evaluated at velocity i (d'Humieres 2002 basis, rows in
+// the order rho, e, eps, jx, qx, jy, qy, jz, qz, 3pxx, 3pixx, pww, piww, pxy,
+// pyz, pxz, mx, my, mz).
+__host__ __device__ constexpr int mrow(int k, int i) {
+  const int x = ex(i), y = ey(i), z = ez(i);
+  const int e2 = x * x + y * y + z * z;
+  switch (k) {
+    case 0: return 1;
+    case 1: return 19 * e2 - 30;
+    case 2: return (21 * e2 * e2 - 53 * e2 + 24) / 2;
+    case 3: return x;
+    case 4: return (5 * e2 - 9) * x;
+    case 5: return y;
+    case 6: return (5 * e2 - 9) * y;
+    case 7: return z;
+    case 8: return (5 * e2 - 9) * z;
+    case 9: return 3 * x * x - e2;
+    case 10: return (3 * e2 - 5) * (3 * x * x - e2);
+    case 11: return y * y - z * z;
+    case 12: return (3 * e2 - 5) * (y * y - z * z);
+    case 13: return x * y;
+    case 14: return y * z;
+    case 15: return x * z;
+    case 16: return (y * y - z * z) * x;
+    case 17: return (z * z - x * x) * y;
+    default: return (x * x - y * y) * z;
+  }
+}
+__host__ __device__ constexpr int mnorm(int k) {
+  int s = 0;
+  for (int i = 0; i < Q; ++i) s += mrow(k, i) * mrow(k, i);
+  return s;
+}
+__host__ __device__ constexpr bool is_stress(int k) {
+  return k == 9 || k == 11 || k == 13 || k == 14 || k == 15;
+}
+__host__ __device__ constexpr bool is_conserved(int k) {
+  return k == 0 || k == 3 || k == 5 || k == 7;
+}
+
+// ---------------------------------------------------------------------------
+// Population storage.  FP32/FP64 store f itself; FP16/BF16 store the deviation
+// f_i - w_i from the rest weights (arithmetic stays FP32).
+// ---------------------------------------------------------------------------
+template <class St> struct Storage;
+template <> struct Storage<float> {
+  using Re = float;
+  static __device__ __forceinline__ float ld(const float* p, float) { return __ldg(p); }
+  static __device__ __forceinline__ void st(float* p, float v, float) { *p = v; }
+};
+template <> struct Storage<double> {
+  using Re = double;
+  static __device__ __forceinline__ double ld(const double* p, double) { return __ldg(p); }
+  static __device__ __forceinline__ void st(double* p, double v, double) { *p = v; }
+};
+template <> struct Storage<__half> {
+  using Re = float;
+  static __device__ __forceinline__ float ld(const __half* p, float w) {
+    return w + __half2float(__ldg(p));
+  }
+  static __device__ __forceinline__ void st(__half* p, float v, float w) {
+    *p = __float2half_rn(v - w);
+  }
+};
+template <> struct Storage<__nv_bfloat16> {
+  using Re = float;
+  static __device__ __forceinline__ float ld(const __nv_bfloat16* p, float w) {
+    return w + __bfloat162float(__ldg(p));
+  }
+  static __device__ __forceinline__ void st(__nv_bfloat16* p, float v, float w) {
+    *p = __float2bfloat16_rn(v - w);
+  }
+};
+
+// Lattice constants handed to kernels by value (constant bank).  ``w`` and
+// ``rate`` are either the reference's float32-rounded values or the exact
+// rationals, chosen on the host.
+template <class Re> struct Consts {
+  Re w[Q];
+  Re rate[Q];   // fixed MRT rates; stress slots are overwritten by omega
+};
+
+// ---------------------------------------------------------------------------
+// Macroscopic moments.
+// ---------------------------------------------------------------------------
+template <class Re>
+__host__ __device__ __forceinline__ Re density(const Re f[Q]) {
+  Re r = f[0];
+#pragma unroll
+  for (int i = 1; i < Q; ++i) r += f[i];
+  return r;
+}
+
+template <class Re>
+__host__ __device__ __forceinline__ void momentum(const Re f[Q], Re& jx, Re& jy, Re& jz) {
+  jx = (f[1] - f[2]) + (f[7] - f[8]) + (f[9] - f[10]) + (f[11] - f[12]) + (f[13] - f[14]);
+  jy = (f[3] - f[4]) + (f[7] + f[8]) - (f[9] + f[10]) + (f[15] - f[16]) + (f[17] - f[18]);
+  jz = (f[5] - f[6]) + (f[11] + f[12]) - (f[13] + f[14]) + (f[15] + f[16]) - (f[17] + f[18]);
+}
+
+// e_i . u for direction i (compile-time i).
+template <class Re>
+__host__ __device__ __forceinline__ Re edotu(int i, Re ux, Re uy, Re uz) {
+  Re s = Re(0);
+  if (ex(i) == 1) s += ux;
+  if (ex(i) == -1) s -= ux;
+  if (ey(i) == 1) s += uy;
+  if (ey(i) == -1) s -= uy;
+  if (ez(i) == 1) s += uz;
+  if (ez(i) == -1) s -= uz;
+  return s;
+}
+
+// f_eq_i = w_i rho (1 + 3 eu + 4.5 eu^2 - 1.5 u^2)   (equilibrium.py:144-149)
+template <class Re>
+__host__ __device__ __forceinline__ void equilibrium(Re rho, Re ux, Re uy, Re uz, const Re w[Q],
+                                            Re feq[Q]) {
+  const Re usq = ux * ux + uy * uy + uz * uz;
+  const Re base = Re(1) - Re(1.5) * usq;
+#pragma unroll
+  for (int i = 0; i < Q; ++i) {
+    const Re eu = edotu<Re>(i, ux, uy, uz);
+    feq[i] = w[i] * rho * (base + eu * (Re(3) + Re(4.5) * eu));
+  }
+}
+
+// Cotangent v on f_eq(rho, u) -> (g_rho, g_u) at fixed (rho, u).
+template <class Re>
+__host__ __device__ __forceinline__ void equilibrium_vjp(const Re v[Q], Re rho, Re ux, Re uy, Re uz,
+                                                const Re w[Q], Re& grho, Re& gx, Re& gy,
+                                                Re& gz) {
+  const Re usq = ux * ux + uy * uy + uz * uz;
+  const Re base = Re(1) - Re(1.5) * usq;
+  Re sp = 0, sw = 0, ax = 0, ay = 0, az = 0;
+#pragma unroll
+  for (int i = 0; i < Q; ++i) {
+    const Re eu = edotu<Re>(i, ux, uy, uz);
+    const Re vw = v[i] * w[i];
+    sp += vw * (base + eu * (Re(3) + Re(4.5) * eu));
+    sw += vw;
+    const Re t = vw * (Re(1) + Re(3) * eu);
+    if (ex(i) == 1) ax += t;
+    if (ex(i) == -1) ax -= t;
+    if (ey(i) == 1) ay += t;
+    if (ey(i) == -1) ay -= t;
+    if (ez(i) == 1) az += t;
+    if (ez(i) == -1) az -= t;
+  }
+  grho = sp;
+  gx = Re(3) * rho * (ax - ux * sw);
+  gy = Re(3) * rho * (ay - uy * sw);
+  gz = Re(3) * rho * (az - uz * sw);
+}
+
+// Chain (g_rho, g_u) through rho = sum f, u = j / rho onto g_f (accumulates).
+template <class Re>
+__host__ __device__ __forceinline__ void macro_vjp_add(Re grho, Re gx, Re gy, Re gz, Re rho, Re ux,
+                                              Re uy, Re uz, Re gf[Q]) {
+  const Re ir = Re(1) / rho;
+  const Re hx = gx * ir, hy = gy * ir, hz = gz * ir;
+  const Re c0 = grho - (hx * ux + hy * uy + hz * uz);
+#pragma unroll
+  for (int i = 0; i < Q; ++i) {
+    Re s = c0;
+    if (ex(i) == 1) s += hx;
+    if (ex(i) == -1) s -= hx;
+    if (ey(i) == 1) s += hy;
+    if (ey(i) == -1) s -= hy;
+    if (ez(i) == 1) s += hz;
+    if (ez(i) == -1) s -= hz;
+    gf[i] += s;
+  }
+}
+
+// ---------------------------------------------------------------------------
+// MRT transforms.  m = M f with shared partial sums; the back transform applies
+// f_i -= sum_k M[k][i] d_k for the 15 non-conserved moments.
+// ---------------------------------------------------------------------------
+template <class Re>
+__host__ __device__ __forceinline__ void mrt_moments(const Re f[Q], Re m[Q]) {
+  const Re a1 = f[1] + f[2], d1 = f[1] - f[2];
+  const Re a3 = f[3] + f[4], d3 = f[3] - f[4];
+  const Re a5 = f[5] + f[6], d5 = f[5] - f[6];
+  const Re pxy = f[7] + f[10], qxy = f[8] + f[9];
+  const Re pxz = f[11] + f[14], qxz = f[12] + f[13];
+  const Re pyz = f[15] + f[18], qyz = f[16] + f[17];
+  const Re sxy = pxy + qxy, sxz = pxz + qxz, syz = pyz + qyz;
+  const Re u1 = f[7] - f[10], u2 = f[9] - f[8];
+  const Re v1 = f[11] - f[14], v2 = f[13] - f[12];
+  const Re w1 = f[15] - f[18], w2 = f[17] - f[16];
+  const Re jx_xy = u1 + u2, jy_xy = u1 - u2;
+  const Re jx_xz = v1 + v2, jz_xz = v1 - v2;
+  const Re jy_yz = w1 + w2, jz_yz = w1 - w2;
+  const Re sf = a1 + a3 + a5;
+  const Re se = sxy + sxz + syz;
+  m[0] = f[0] + sf + se;
+  m[1] = Re(-30) * f[0] - Re(11) * sf + Re(8) * se;
+  m[2] = Re(12) * f[0] - Re(4) * sf + se;
+  m[3] = d1 + jx_xy + jx_xz;
+  m[4] = Re(-4) * d1 + jx_xy + jx_xz;
+  m[5] = d3 + jy_xy + jy_yz;
+  m[6] = Re(-4) * d3 + jy_xy + jy_yz;
+  m[7] = d5 + jz_xz + jz_yz;
+  m[8] = Re(-4) * d5 + jz_xz + jz_yz;
+  const Re t9 = sxy + sxz - Re(2) * syz;
+  m[9] = Re(2) * a1 - a3 - a5 + t9;
+  m[10] = Re(-4) * a1 + Re(2) * (a3 + a5) + t9;
+  const Re t11 = sxy - sxz;
+  m[11] = a3 - a5 + t11;
+  m[12] = Re(-2) * (a3 - a5) + t11;
+  m[13] = pxy - qxy;
+  m[14] = pyz - qyz;
+  m[15] = pxz - qxz;
+  m[16] = jx_xy - jx_xz;
+  m[17] = jy_yz - jy_xy;
+  m[18] = jz_xz - jz_yz;
+}
+
+// out_i = in_i - sum_{k non-conserved} M[k][i] d_k
+template <class Re>
+__host__ __device__ __forceinline__ void mrt_back(const Re d[Q], const Re in[Q], Re out[Q]) {
+  const Re cf = Re(-11) * d[1] - Re(4) * d[2];
+  const Re ce = Re(8) * d[1] + d[2];
+  const Re fx = Re(2) * d[9] - Re(4) * d[10];
+  const Re fy = -d[9] + Re(2) * d[10] + d[11] - Re(2) * d[12];
+  const Re fz = -d[9] + Re(2) * d[10] - d[11] + Re(2) * d[12];
+  const Re exy = ce + d[9] + d[10] + d[11] + d[12];
+  const Re exz = ce + d[9] + d[10] - d[11] - d[12];
+  const Re eyz = ce - Re(2) * (d[9] + d[10]);
+  out[0] = in[0] - (Re(-30) * d[1] + Re(12) * d[2]);
+  out[1] = in[1] - (cf + fx - Re(4) * d[4]);
+  out[2] = in[2] - (cf + fx + Re(4) * d[4]);
+  out[3] = in[3] - (cf + fy - Re(4) * d[6]);
+  out[4] = in[4] - (cf + fy + Re(4) * d[6]);
+  out[5] = in[5] - (cf + fz - Re(4) * d[8]);
+  out[6] = in[6] - (cf + fz + Re(4) * d[8]);
+  // xy edges: rows 4, 6, 13, 16, 17
+  const Re a46p = d[4] + d[6], a46m = d[4] - d[6];
+  const Re b1617p = d[16] + d[17], b1617m = d[16] - d[17];
+  out[7] = in[7] - (exy + a46p + d[13] + b1617m);
+  out[8] = in[8] - (exy - a46m - d[13] - b1617p);
+  out[9] = in[9] - (exy + a46m - d[13] + b1617p);
+  out[10] = in[10] - (exy - a46p + d[13] - b1617m);
+  // xz edges: rows 4, 8, 15, 16, 18
+  const Re a48p = d[4] + d[8], a48m = d[4] - d[8];
+  const Re b1618p = d[16] + d[18], b1618m = d[16] - d[18];
+  out[11] = in[11] - (exz + a48p + d[15] - b1618m);
+  out[12] = in[12] - (exz - a48m - d[15] + b1618p);
+  out[13] = in[13] - (exz + a48m - d[15] - b1618p);
+  out[14] = in[14] - (exz - a48p + d[15] + b1618m);
+  // yz edges: rows 6, 8, 14, 17, 18
+  const Re a68p = d[6] + d[8], a68m = d[6] - d[8];
+  const Re b1718p = d[17] + d[18], b1718m = d[17] - d[18];
+  out[15] = in[15] - (eyz + a68p + d[14] + b1718m);
+  out[16] = in[16] - (eyz - a68m - d[14] - b1718p);
+  out[17] = in[17] - (eyz + a68m - d[14] + b1718p);
+  out[18] = in[18] - (eyz - a68p + d[14] - b1718m);
+}
+
+// Equilibrium moments (lattice.py:342-391) for the non-conserved rows.
+template <class Re>
+__host__ __device__ __forceinline__ void mrt_meq(Re rho, Re ux, Re uy, Re uz, Re meq[Q]) {
+  const Re u2 = ux * ux + uy * uy + uz * uz;
+  const Re pxx = Re(2) * ux * ux - uy * uy - uz * uz;
+  const Re pww = uy * uy - uz * uz;
+  meq[0] = rho;
+  meq[1] = rho * (Re(-11) + Re(19) * u2);
+  meq[2] = rho * (Re(3) - Re(5.5) * u2);
+  meq[3] = rho * ux;
+  meq[4] = Re(-2.0 / 3.0) * rho * ux;
+  meq[5] = rho * uy;
+  meq[6] = Re(-2.0 / 3.0) * rho * uy;
+  meq[7] = rho * uz;
+  meq[8] = Re(-2.0 / 3.0) * rho * uz;
+  meq[9] = rho * pxx;
+  meq[10] = Re(-0.5) * rho * pxx;
+  meq[11] = rho * pww;
+  meq[12] = Re(-0.5) * rho * pww;
+  meq[13] = rho * ux * uy;
+  meq[14] = rho * uy * uz;
+  meq[15] = rho * ux * uz;
+  meq[16] = Re(0);
+  meq[17] = Re(0);
+  meq[18] = Re(0);
+}
+
+// ---------------------------------------------------------------------------
+// Smagorinsky: tau_eff = (tau + sqrt(tau^2 + c Pi / (rho + 1e-10))) / 2 with
+// c = 18 Cs^2 and Pi the Frobenius norm of the non-equilibrium stress
+// Pi_ab = sum_i e_ia e_ib (f_i - feq_i) (collision.py:187-270).  The
+// equilibrium part is evaluated in closed form, sum_i e_ia e_ib feq_i =
+// rho/3 delta_ab + rho u_a u_b, from the raw second moments of f.
+// ---------------------------------------------------------------------------
+template <class Re>
+__host__ __device__ __forceinline__ void raw_second_moments(const Re f[Q], Re p[6]) {
+  const Re a1 = f[1] + f[2], a3 = f[3] + f[4], a5 = f[5] + f[6];
+  const Re sxy = (f[7] + f[10]) + (f[8] + f[9]);
+  const Re sxz = (f[11] + f[14]) + (f[12] + f[13]);
+  const Re syz = (f[15] + f[18]) + (f[16] + f[17]);
+  p[0] = a1 + sxy + sxz;                       // sum ex^2 f
+  p[1] = a3 + sxy + syz;                       // sum ey^2 f
+  p[2] = a5 + sxz + syz;                       // sum ez^2 f
+  p[3] = (f[7] + f[10]) - (f[8] + f[9]);       // sum ex ey f
+  p[4] = (f[11] + f[14]) - (f[12] + f[13]);    // sum ex ez f
+  p[5] = (f[15] + f[18]) - (f[16] + f[17]);    // sum ey ez f
+}
+
+// Non-equilibrium stress from raw second moments p and (rho, u).
+template <class Re>
+__host__ __device__ __forceinline__ void neq_stress(const Re p[6], Re rho, Re ux, Re uy, Re uz,
+                                                    Re s[6]) {
+  const Re r3 = rho * Re(1.0 / 3.0);
+  s[0] = p[0] - (r3 + rho * ux * ux);
+  s[1] = p[1] - (r3 + rho * uy * uy);
+  s[2] = p[2] - (r3 + rho * uz * uz);
+  s[3] = p[3] - rho * ux * uy;
+  s[4] = p[4] - rho * ux * uz;
+  s[5] = p[5] - rho * uy * uz;
+}
+
+template <class Re>
+__host__ __device__ __forceinline__ Re smag_pi(const Re s[6]) {
+  return sqrt(s[0] * s[0] + s[1] * s[1] + s[2] * s[2] +
+              Re(2) * (s[3] * s[3] + s[4] * s[4] + s[5] * s[5]));
+}
+
+// 1 / (rho + 1e-10): in float the epsilon is below half an ulp of any
+// physical density, so the reciprocal of rho is reused.
+template <class Re>
+__host__ __device__ __forceinline__ Re inv_rho_eps(Re rho, Re inv_rho) {
+  if (sizeof(Re) == 4) return inv_rho;
+  return Re(1) / (rho + Re(1e-10));
+}
+
+template <class Re>
+__host__ __device__ __forceinline__ Re smag_tau(Re tau, Re c18cs2, Re pi, Re inv_rr) {
+  return Re(0.5) * (tau + sqrt(tau * tau + c18cs2 * pi * inv_rr));
+}
+
+// ---------------------------------------------------------------------------
+// Collision forward.  ``omega`` = 1 / tau_eff.  BGK: f - omega (f - f_eq).
+// MRT: f - M^-1 S (M f - m_eq), with S = rates and omega in the stress slots.
+// ---------------------------------------------------------------------------
+template <class Re>
+__host__ __device__ __forceinline__ void bgk_collide(const Re f[Q], Re rho, Re ux, Re uy, Re uz,
+                                            Re omega, const Re w[Q], Re out[Q]) {
+  Re feq[Q];
+  equilibrium<Re>(rho, ux, uy, uz, w, feq);
+#pragma unroll
+  for (int i = 0; i < Q; ++i) out[i] = f[i] - omega * (f[i] - feq[i]);
+}
+
+template <class Re>
+__host__ __device__ __forceinline__ void mrt_relax_back(const Re f[Q], const Re m[Q], Re rho,
+                                                        Re ux, Re uy, Re uz, Re omega,
+                                                        const Re rate[Q], Re out[Q]) {
+  Re meq[Q], d[Q];
+  mrt_meq<Re>(rho, ux, uy, uz, meq);
+  const Re on = omega;
+#pragma unroll
+  for (int k = 0; k < Q; ++k) {
+    const Re s = is_stress(k) ? on : rate[k];
+    d[k] = is_conserved(k) ? Re(0) : (s * Re(1.0 / double(mnorm(k)))) * (m[k] - meq[k]);
+  }
+  mrt_back<Re>(d, f, out);
+}
+
+template <class Re>
+__host__ __device__ __forceinline__ void mrt_collide(const Re f[Q], Re rho, Re ux, Re uy, Re uz,
+                                            Re omega, const Re rate[Q], Re out[Q]) {
+  Re m[Q];
+  mrt_moments<Re>(f, m);
+  mrt_relax_back<Re>(f, m, rho, ux, uy, uz, omega, rate, out);
+}
+
+// Full collide of one cell given its density and momentum: optional
+// Smagorinsky tau, then BGK/MRT.  Returns omega actually used.
+template <class Re>
+__host__ __device__ __forceinline__ Re collide_cell_rj(const Re f[Q], Re rho, Re jx, Re jy, Re jz,
+                                                       Re tau, bool mrt, bool smag, Re c18cs2,
+                                                       const Consts<Re>& K, Re out[Q]) {
+  const Re ir = Re(1) / rho;
+  const Re ux = jx * ir, uy = jy * ir, uz = jz * ir;
+  Re omega;
+  if (mrt) {
+    Re m[Q];
+    mrt_moments<Re>(f, m);
+    if (smag) {
+      // raw second moments from the MRT partial sums: sum ex^2 f = (m0 + ... )
+      Re p[6], s[6];
+      raw_second_moments<Re>(f, p);
+      neq_stress<Re>(p, rho, ux, uy, uz, s);
+      omega = Re(1) / smag_tau<Re>(tau, c18cs2, smag_pi<Re>(s), inv_rho_eps<Re>(rho, ir));
+    } else {
+      omega = Re(1) / tau;
+    }
+    mrt_relax_back<Re>(f, m, rho, ux, uy, uz, omega, K.rate, out);
+  } else {
+    if (smag) {
+      Re p[6], s[6];
+      raw_second_moments<Re>(f, p);
+      neq_stress<Re>(p, rho, ux, uy, uz, s);
+      omega = Re(1) / smag_tau<Re>(tau, c18cs2, smag_pi<Re>(s), inv_rho_eps<Re>(rho, ir));
+    } else {
+      omega = Re(1) / tau;
+    }
+    bgk_collide<Re>(f, rho, ux, uy, uz, omega, K.w, out);
+  }
+  return omega;
+}
+
+template <class Re>
+__host__ __device__ __forceinline__ Re collide_cell(const Re f[Q], Re tau, bool mrt, bool smag,
+                                                    Re c18cs2, const Consts<Re>& K, Re out[Q]) {
+  Re jx, jy, jz;
+  momentum<Re>(f, jx, jy, jz);
+  return collide_cell_rj<Re>(f, density<Re>(f), jx, jy, jz, tau, mrt, smag, c18cs2, K, out);
+}
+
+// ---------------------------------------------------------------------------
+// Collision VJP.  Given the pre-collision f and the cotangent lam on the
+// collide output, returns gf = (d collide / d f)^T lam, and g_tau (cotangent of
+// the base tau of this cell; through Smagorinsky when enabled).
+//
+// Smagorinsky: d Pi / d s is undefined at Pi = 0 (jax.grad yields NaN there);
+// this implementation uses the subgradient 0.
+// ---------------------------------------------------------------------------
+template <class Re>
+__host__ __device__ __forceinline__ void collide_vjp(const Re f[Q], const Re lam[Q], Re tau,
+                                                     bool mrt, bool smag, Re c18cs2,
+                                                     const Consts<Re>& K, Re gf[Q],
+                                                     Re* g_tau_out) {
+  const Re rho = density<Re>(f);
+  Re jx, jy, jz;
+  momentum<Re>(f, jx, jy, jz);
+  const Re ir = Re(1) / rho;
+  const Re ux = jx * ir, uy = jy * ir, uz = jz * ir;
+  Re sst[6];
+  Re tau_eff = tau, pi = Re(0), R = Re(0), inv_rr = Re(0);
+  if (smag) {
+    Re p[6];
+    raw_second_moments<Re>(f, p);
+    neq_stress<Re>(p, rho, ux, uy, uz, sst);
+    pi = smag_pi<Re>(sst);
+    inv_rr = inv_rho_eps<Re>(rho, ir);
+    R = sqrt(tau * tau + c18cs2 * pi * inv_rr);
+    tau_eff = Re(0.5) * (tau + R);
+  }
+  const Re omega = Re(1) / tau_eff;
+  Re g_omega = Re(0);
+  Re grho = 0, gx = 0, gy = 0, gz = 0;
+  if (mrt) {
+    Re ml[Q], g[Q], m[Q], meq[Q];
+    mrt_moments<Re>(lam, ml);
+    mrt_moments<Re>(f, m);
+    mrt_meq<Re>(rho, ux, uy, uz, meq);
+#pragma unroll
+    for (int k = 0; k < Q; ++k) {
+      const Re s = is_stress(k) ? omega : K.rate[k];
+      const Re pk = ml[k] * Re(1.0 / double(mnorm(k)));
+      g[k] = is_conserved(k) ? Re(0) : s * pk;
+      if (is_stress(k)) g_omega -= pk * (m[k] - meq[k]);
+    }
+    // gf = lam - M^T g
+    mrt_back<Re>(g, lam, gf);
+    // + (d m_eq / d f)^T g, via (rho, u)
+    const Re a9 = g[9] - Re(0.5) * g[10];
+    const Re a11 = g[11] - Re(0.5) * g[12];
+    const Re u2 = ux * ux + uy * uy + uz * uz;
+    const Re pxx = Re(2) * ux * ux - uy * uy - uz * uz;
+    const Re pww = uy * uy - uz * uz;
+    grho = g[1] * (Re(-11) + Re(19) * u2) + g[2] * (Re(3) - Re(5.5) * u2) +
+           Re(-2.0 / 3.0) * (g[4] * ux + g[6] * uy + g[8] * uz) + a9 * pxx + a11 * pww +
+           g[13] * ux * uy + g[14] * uy * uz + g[15] * ux * uz;
+    const Re q12 = Re(38) * g[1] - Re(11) * g[2];
+    gx = rho * (q12 * ux + Re(-2.0 / 3.0) * g[4] + Re(4) * a9 * ux + g[13] * uy + g[15] * uz);
+    gy = rho * (q12 * uy + Re(-2.0 / 3.0) * g[6] - Re(2) * a9 * uy + Re(2) * a11 * uy +
+                g[13] * ux + g[14] * uz);
+    gz = rho * (q12 * uz + Re(-2.0 / 3.0) * g[8] - Re(2) * a9 * uz - Re(2) * a11 * uz +
+                g[14] * uy + g[15] * ux);
+  } else {
+    Re feq[Q], v[Q];
+    equilibrium<Re>(rho, ux, uy, uz, K.w, feq);
+#pragma unroll
+    for (int i = 0; i < Q; ++i) {
+      gf[i] = (Re(1) - omega) * lam[i];
+      v[i] = omega * lam[i];
+      g_omega -= lam[i] * (f[i] - feq[i]);
+    }
+    equilibrium_vjp<Re>(v, rho, ux, uy, uz, K.w, grho, gx, gy, gz);
+  }
+  macro_vjp_add<Re>(grho, gx, gy, gz, rho, ux, uy, uz, gf);
+
+  // omega = 1 / tau_eff
+  const Re g_tau_eff = -g_omega * omega * omega;
+  Re g_tau = g_tau_eff;
+  if (smag) {
+    // tau_eff = (tau + R)/2, R = sqrt(tau^2 + c pi inv_rr)
+    const Re gR = Re(0.5) * g_tau_eff;
+    const Re gX = (R > Re(0)) ? gR / (Re(2) * R) : Re(0);
+    g_tau = Re(0.5) * g_tau_eff + gX * Re(2) * tau;
+    const Re g_pi = gX * c18cs2 * inv_rr;
+    const Re g_rho_direct = -gX * c18cs2 * pi * inv_rr * inv_rr;
+    if (pi > Re(0)) {
+      // d pi / d s (s = xx, yy, zz, xy, xz, yz; off-diagonals counted twice)
+      const Re ip = g_pi / pi;
+      const Re gs0 = ip * sst[0], gs1 = ip * sst[1], gs2 = ip * sst[2];
+      const Re gs3 = Re(2) * ip * sst[3], gs4 = Re(2) * ip * sst[4], gs5 = Re(2) * ip * sst[5];
+      // s_ab = p_ab(f) - rho/3 delta_ab - j_a j_b / rho
+      const Re t2 = -(gs0 + gs1 + gs2) * Re(1.0 / 3.0) +
+                    (gs0 * ux * ux + gs1 * uy * uy + gs2 * uz * uz + gs3 * ux * uy +
+                     gs4 * ux * uz + gs5 * uy * uz);
+      const Re bx = Re(2) * gs0 * ux + gs3 * uy + gs4 * uz;
+      const Re by = Re(2) * gs1 * uy + gs3 * ux + gs5 * uz;
+      const Re bz = Re(2) * gs2 * uz + gs4 * ux + gs5 * uy;
+#pragma unroll
+      for (int i = 0; i < Q; ++i) {
+        const int x = ex(i), y = ey(i), z = ez(i);
+        Re t = t2;
+        if (x != 0) t += gs0 - Re(x) * bx;
+        if (y != 0) t += gs1 - Re(y) * by;
+        if (z != 0) t += gs2 - Re(z) * bz;
+        if (x * y != 0) t += Re(x * y) * gs3;
+        if (x * z != 0) t += Re(x * z) * gs4;
+        if (y * z != 0) t += Re(y * z) * gs5;
+        gf[i] += t;
+      }
+    }
+#pragma unroll
+    for (int i = 0; i < Q; ++i) gf[i] += g_rho_direct;
+  }
+  if (g_tau_out) *g_tau_out = g_tau;
+}
+
+}  // namespace lbm

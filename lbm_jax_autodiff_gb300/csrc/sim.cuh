@@ -1,0 +1,186 @@
+// Shared device-side structures of the fused solver: grid, boundary-cell
+// records, kernel argument blocks and the pull / Bouzidi / Zou-He helpers.
+//
+// Data layout in HBM (identical to jax_lbm's arrays, state.py:41-44):
+//   populations  [19][nx][ny][nz]  z fastest (structure of arrays)
+//   tag          [nx][ny][nz] uint32: bit 31 = hard-solid cell, bits 0..30 =
+//                1 + index of the cell's LinkRec (0 = plain cell)
+//   LinkRec[]    one record per "special" cell: a cell that owns a Bouzidi
+//                link, is the target of one, or is the second fluid cell of a
+//                q < 0.5 link.  Only these cells read anything beyond the pull.
+#pragma once
+
+#include "lbm_core.cuh"
+
+namespace lbm {
+
+constexpr uint32_t TAG_SOLID = 0x80000000u;
+constexpr uint32_t TAG_INDEX = 0x7FFFFFFFu;
+
+struct alignas(16) LinkRec {
+  uint32_t linkmask;  // bit j: q[j](x) >= 0  (direction j from x hits a wall)
+  uint32_t nb_wall;   // bit j: pull neighbour x+e_j has q[opp j] >= 0
+  uint32_t nb_low;    // bit j: 0 <= q[j](wrap(x+e_j)) < 0.5
+  uint32_t pad;
+  double q[Q];        // q[j](x)
+  double qnb[Q];      // q[j](wrap(x+e_j)) for nb_low bits
+  double dqdr[Q];     // d q[j](x) / d r
+};
+
+struct Grid {
+  int nx, ny, nz;
+  int n;              // nx*ny*nz
+  int periodic_yz;
+};
+
+// flags of StepArgs::flags
+enum : int {
+  SF_SMAG = 1 << 0,
+  SF_SOLID_HARD = 1 << 1,
+  SF_SOLID_SPHERE = 1 << 2,   // analytic sigmoid porosity
+  SF_SOLID_FIELD = 1 << 3,    // porosity array
+  SF_GUARD_PRE = 1 << 4,
+  SF_GUARD_POST = 1 << 5,
+  SF_FORCE = 1 << 6,
+  SF_COLLIDE_ONLY = 1 << 7,   // input is the reference-layout f (no pull)
+  SF_STREAM_ONLY = 1 << 8,    // output is the reference-layout post-BC f
+  SF_INLET_FACE = 1 << 9,     // per-(y,z) inlet velocity
+  SF_NO_INLET = 1 << 10,
+  SF_NO_OUTLET = 1 << 11,
+};
+
+template <class Re> struct SphereP {
+  Re c[3];
+  Re r;
+  Re alpha;
+  Re sx, sy, sz;   // cells per world unit: nx/8, ny/4, nz/4
+};
+
+template <class Re> struct StepArgs {
+  const void* src;        // populations S_{k-1} (storage type) or f_0 (Re)
+  void* dst;              // populations S_k (storage type) or post-BC f (Re)
+  const uint32_t* tag;
+  const LinkRec* rec;
+  Grid g;
+  Consts<Re> K;
+  Re tau;
+  Re c18cs2;              // 18 Cs^2
+  int flags;
+  Re u_in[3];
+  const Re* u_face;       // [3][ny][nz]
+  Re rho_out;
+  SphereP<Re> sph;
+  const Re* porosity;     // [n]
+  Re guard_reset[Q];
+  double* force_partials; // [gridDim.x][3]
+  unsigned long long* guard_count;
+};
+
+__device__ __forceinline__ int wrapi(int v, int n) { return v < 0 ? v + n : (v >= n ? v - n : v); }
+
+// Pull source of direction i for cell (x,y,z) following streaming.py:109-142:
+// x is never periodic, y/z are periodic or clamped; any out-of-range axis
+// makes the cell keep its own value.
+__device__ __forceinline__ int pull_src(int i, const Grid& g, int idx, int x, int y, int z) {
+  int sx = x - ex(i), sy = y - ey(i), sz = z - ez(i);
+  bool fb = false;
+  if (ex(i) != 0) fb |= (sx < 0) | (sx >= g.nx);
+  if (ey(i) != 0) {
+    if (g.periodic_yz) sy = wrapi(sy, g.ny); else fb |= (sy < 0) | (sy >= g.ny);
+  }
+  if (ez(i) != 0) {
+    if (g.periodic_yz) sz = wrapi(sz, g.nz); else fb |= (sz < 0) | (sz >= g.nz);
+  }
+  return fb ? idx : ((sx * g.ny + sy) * g.nz + sz);
+}
+
+// Cell x + e_i wrapped in all three axes (jnp.roll semantics, streaming.py:166-172).
+__device__ __forceinline__ int ahead_wrap(const Grid& g, int x, int y, int z, int dx, int dy,
+                                          int dz) {
+  return (wrapi(x + dx, g.nx) * g.ny + wrapi(y + dy, g.ny)) * g.nz + wrapi(z + dz, g.nz);
+}
+
+// Zou-He velocity inlet at x = 0 (boundary.py:35-124).
+template <class Re>
+__device__ __forceinline__ void zou_he_inlet(Re f[Q], Re ux, Re uy, Re uz) {
+  const Re k0 = f[0] + f[3] + f[4] + f[5] + f[6] + f[15] + f[16] + f[17] + f[18];
+  const Re kn = f[2] + f[8] + f[10] + f[12] + f[14];
+  const Re rho = (k0 + Re(2) * kn) / (Re(1) - ux);
+  const Re c3 = Re(1.0 / 3.0) * rho, c6 = Re(1.0 / 6.0) * rho;
+  f[1] = f[2] + c3 * ux;
+  f[7] = f[10] + c6 * (ux + uy);
+  f[9] = f[8] + c6 * (ux - uy);
+  f[11] = f[14] + c6 * (ux + uz);
+  f[13] = f[12] + c6 * (ux - uz);
+}
+
+// Zou-He pressure outlet at x = nx-1 with u_y = u_z = 0 (boundary.py:127-200).
+template <class Re>
+__device__ __forceinline__ void zou_he_outlet(Re f[Q], Re rho_out) {
+  const Re k0 = f[0] + f[3] + f[4] + f[5] + f[6] + f[15] + f[16] + f[17] + f[18];
+  const Re kp = f[1] + f[7] + f[9] + f[11] + f[13];
+  const Re ux = Re(-1) + (k0 + Re(2) * kp) / rho_out;
+  const Re c3 = Re(1.0 / 3.0) * rho_out * ux, c6 = Re(1.0 / 6.0) * rho_out * ux;
+  f[2] = f[1] - c3;
+  f[10] = f[7] - c6;
+  f[8] = f[9] - c6;
+  f[14] = f[11] - c6;
+  f[12] = f[13] - c6;
+}
+
+// Sigmoid porosity of the analytic sphere at cell (x,y,z), smooth.py:34-115:
+// p = sigmoid(alpha (r - |x_world - c|)).
+template <class Re>
+__device__ __forceinline__ Re sphere_porosity(const SphereP<Re>& s, int x, int y, int z,
+                                              Re* dpdr) {
+  const Re wx = (Re(x) + Re(0.5)) / s.sx - Re(4);
+  const Re wy = (Re(y) + Re(0.5)) / s.sy - Re(2);
+  const Re wz = (Re(z) + Re(0.5)) / s.sz - Re(2);
+  const Re dx = wx - s.c[0], dy = wy - s.c[1], dz = wz - s.c[2];
+  const Re d = sqrt(dx * dx + dy * dy + dz * dz);
+  const Re p = Re(1) / (Re(1) + exp(-s.alpha * (s.r - d)));
+  if (dpdr) *dpdr = s.alpha * p * (Re(1) - p);
+  return p;
+}
+
+// Guard test of state.py:161-166 / examples/10:164-167 on (rho, j).
+template <class Re>
+__device__ __forceinline__ bool unstable_rj(Re rho, Re jx, Re jy, Re jz) {
+  const Re ir = Re(1) / rho;
+  const Re ux = jx * ir, uy = jy * ir, uz = jz * ir;
+  const Re um = sqrt(ux * ux + uy * uy + uz * uz);
+  return (rho < Re(0.3)) || (rho > Re(2.0)) || (um > Re(0.4)) || (rho != rho);
+}
+
+// Block-wide sum of three doubles; thread 0 writes them to out[blockIdx.x*3].
+__device__ __forceinline__ void block_sum3_store(double a, double b, double c, double* out) {
+  __shared__ double sh[3][32];
+#pragma unroll
+  for (int o = 16; o > 0; o >>= 1) {
+    a += __shfl_down_sync(0xffffffffu, a, o);
+    b += __shfl_down_sync(0xffffffffu, b, o);
+    c += __shfl_down_sync(0xffffffffu, c, o);
+  }
+  const int lane = threadIdx.x & 31, wid = threadIdx.x >> 5;
+  if (lane == 0) { sh[0][wid] = a; sh[1][wid] = b; sh[2][wid] = c; }
+  __syncthreads();
+  if (wid == 0) {
+    const int nw = (blockDim.x + 31) >> 5;
+    a = lane < nw ? sh[0][lane] : 0.0;
+    b = lane < nw ? sh[1][lane] : 0.0;
+    c = lane < nw ? sh[2][lane] : 0.0;
+#pragma unroll
+    for (int o = 16; o > 0; o >>= 1) {
+      a += __shfl_down_sync(0xffffffffu, a, o);
+      b += __shfl_down_sync(0xffffffffu, b, o);
+      c += __shfl_down_sync(0xffffffffu, c, o);
+    }
+    if (lane == 0) {
+      out[3 * blockIdx.x + 0] = a;
+      out[3 * blockIdx.x + 1] = b;
+      out[3 * blockIdx.x + 2] = c;
+    }
+  }
+}
+
+}  // namespace lbm
