@@ -121,6 +121,20 @@ int lbm_get_state(lbm_sim* sim, void* f, void* stream);
  * momentum_exchange(f_post, f, q) + drag_coefficient (forces.py:37-120,237-276). */
 int lbm_run(lbm_sim* sim, int n_steps, int sample_every, double* samples, void* stream);
 
+/* Shape gradient: from the state set by lbm_set_state, run n_steps and return
+ * Cd = drag_coefficient(momentum_exchange(f_post_last, f_final, q)) and its
+ * derivative with respect to the sphere radius (through the ray-sphere q(r)
+ * and the sigmoid porosity), as jax.grad of the reference drivers'
+ * simulate_cd (examples/11:139-176, examples/08:69-93, tests/
+ * test_gradients_f64.py:154-207).  The hand-written adjoint runs backwards
+ * with populations checkpointed every `checkpoint_every` steps (<= 0: store
+ * every step) and recomputed segment by segment (examples/08:49-66 does the
+ * same with jax.checkpoint).  Optional outputs (device, compute dtype, NULL to
+ * skip): dcd_dq [19][n] = dCd/dq on every link, dcd_df0 [19][n] = dCd/df_0.
+ * Requires guard = LBM_GUARD_OFF.  Synchronises `stream`. */
+int lbm_cd_and_grad(lbm_sim* sim, int n_steps, int checkpoint_every, double* cd_host,
+                    double* dcd_dr_host, void* dcd_dq, void* dcd_df0, void* stream);
+
 /* Host-side queries (synchronise `stream`). */
 int lbm_get_projected_area(lbm_sim* sim, double* area_host);
 int lbm_get_link_count(lbm_sim* sim, int* links_host, int* special_cells_host);

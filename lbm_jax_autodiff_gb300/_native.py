@@ -95,6 +95,7 @@ SIGNATURES = {
     "lbm_set_state": [_vp, _vp, _vp],
     "lbm_get_state": [_vp, _vp, _vp],
     "lbm_run": [_vp, _i, _i, _vp, _vp],
+    "lbm_cd_and_grad": [_vp, _i, _i, ctypes.POINTER(_d), ctypes.POINTER(_d), _vp, _vp, _vp],
     "lbm_get_projected_area": [_vp, ctypes.POINTER(_d)],
     "lbm_get_link_count": [_vp, ctypes.POINTER(_i), ctypes.POINTER(_i)],
     "lbm_get_guard_resets": [_vp, ctypes.POINTER(ctypes.c_ulonglong), _vp],

@@ -1,0 +1,393 @@
+// Adjoint (reverse-mode) time step of the fused solver: the hand-derived
+// transpose of one forward step, giving dCd/dr and dCd/dq without storing
+// any per-step intermediate beyond the populations S_k.
+//
+// Forward (one step k):  f_k = Z(T_q(S_{k-1})),  S_k = B_p(C(f_k))
+//   T_q : pull streaming + Bouzidi with wall distances q   streaming.py:40-185
+//   Z   : Zou-He inlet / outlet (affine in f)              boundary.py:35-200
+//   C   : BGK / MRT collision (+ Smagorinsky)               collision.py:46-270
+//   B_p : hard bounce-back or sigmoid-porosity blend        smooth.py:118-155
+// Objective: Cd(F(S_{N-1}, f_N)) with the momentum-exchange force F
+// (forces.py:37-120, 237-276) -- the reference drivers' simulate_cd
+// (examples/11:139-165) whose gradient jax.grad derives.
+//
+// Adjoint state stored between launches: nu_k = Z^T lambda_k, the cotangent
+// of the streamed (pre-boundary) populations of step k.  One launch of
+// k_adjoint for step k does, per cell y:
+//   mu_k(y)  = (T_q^T nu_{k+1})(y)      gather form of the transposed stream
+//   f_k(y)   = recomputed from the stashed S_{k-1}
+//   dJ/dp   += mu_k . dB/dp  (sigmoid porosity, dp/dr = alpha p (1-p))
+//   dJ/dq   += nu_{k+1} . dT/dq (S_k), per wall link, times dq/dr
+//   lambda_k = C^T B^T mu_k;  nu_k = Z^T lambda_k on the inlet/outlet faces
+#include "capi_util.cuh"
+#include "sim.cuh"
+
+namespace lbm {
+
+template <class Re> struct AdjArgs {
+  StepArgs<Re> s;          // forward description; s.src = S_{k-1} (or f_0 when first)
+  const void* S_k;         // stashed S_k (storage type), for q < 0.5 neighbour reads
+  const Re* nu_in;         // nu_{k+1}
+  Re* nu_out;              // nu_k (lambda_0 when first)
+  int first;               // k == 0
+  int last;                // k == N-1: add dJ/dS_{N-1} of the momentum exchange
+  const double* dj_dfx;    // device scalar dJ/dFx
+  double* gr_partials;     // [gridDim.x] running dJ/dr per block
+  double* gq;              // [nrec][19] running dJ/dq per link
+};
+
+// Zou-He transposes (affine maps; see boundary.py:95-122 and :176-198).
+template <class Re>
+__device__ __forceinline__ void zou_he_inlet_T(Re l[Q], Re ux, Re uy, Re uz) {
+  const Re c3 = Re(1.0 / 3.0), c6 = Re(1.0 / 6.0);
+  const Re grho = c3 * ux * l[1] + c6 * (ux + uy) * l[7] + c6 * (ux - uy) * l[9] +
+                  c6 * (ux + uz) * l[11] + c6 * (ux - uz) * l[13];
+  const Re d = grho / (Re(1) - ux);
+  Re o[Q];
+#pragma unroll
+  for (int j = 0; j < Q; ++j) o[j] = l[j];
+  o[1] = o[7] = o[9] = o[11] = o[13] = Re(0);
+  o[2] += l[1];
+  o[10] += l[7];
+  o[8] += l[9];
+  o[14] += l[11];
+  o[12] += l[13];
+  o[0] += d; o[3] += d; o[4] += d; o[5] += d; o[6] += d;
+  o[15] += d; o[16] += d; o[17] += d; o[18] += d;
+  o[2] += Re(2) * d; o[8] += Re(2) * d; o[10] += Re(2) * d; o[12] += Re(2) * d;
+  o[14] += Re(2) * d;
+#pragma unroll
+  for (int j = 0; j < Q; ++j) l[j] = o[j];
+}
+
+template <class Re>
+__device__ __forceinline__ void zou_he_outlet_T(Re l[Q], Re rho_out) {
+  const Re c3 = Re(1.0 / 3.0), c6 = Re(1.0 / 6.0);
+  const Re gu = -rho_out * (c3 * l[2] + c6 * (l[10] + l[8] + l[14] + l[12]));
+  const Re d = gu / rho_out;
+  Re o[Q];
+#pragma unroll
+  for (int j = 0; j < Q; ++j) o[j] = l[j];
+  o[2] = o[10] = o[8] = o[14] = o[12] = Re(0);
+  o[1] += l[2];
+  o[7] += l[10];
+  o[9] += l[8];
+  o[11] += l[14];
+  o[13] += l[12];
+  o[0] += d; o[3] += d; o[4] += d; o[5] += d; o[6] += d;
+  o[15] += d; o[16] += d; o[17] += d; o[18] += d;
+  o[1] += Re(2) * d; o[7] += Re(2) * d; o[9] += Re(2) * d; o[11] += Re(2) * d;
+  o[13] += Re(2) * d;
+#pragma unroll
+  for (int j = 0; j < Q; ++j) l[j] = o[j];
+}
+
+template <class St, bool MRT>
+__global__ void __launch_bounds__(256, sizeof(St) == 8 ? 1 : 2) k_adjoint(const AdjArgs<typename Storage<St>::Re> A) {
+  using Re = typename Storage<St>::Re;
+  using S = Storage<St>;
+  const StepArgs<Re>& a = A.s;
+  const Grid& g = a.g;
+  const int n = g.n;
+  const int idx = blockIdx.x * blockDim.x + threadIdx.x;
+  const int fl = a.flags;
+  double gr = 0.0;
+
+  if (idx < n) {
+    const int z = idx % g.nz;
+    const int t = idx / g.nz;
+    const int y = t % g.ny;
+    const int x = t / g.ny;
+    const uint32_t tag = a.tag ? __ldg(a.tag + idx) : 0u;
+    const uint32_t ri = tag & TAG_INDEX;
+    const size_t N = size_t(n);
+    const Re* nu = A.nu_in;
+    const PullIdx P(g, x, y, z);
+
+    // ---- mu_k = T^T nu_{k+1}: normal-stream part -----------------------
+    Re mu[Q];
+    mu[0] = __ldg(nu + idx);
+#pragma unroll
+    for (int j = 1; j < Q; ++j) {
+      // (a) output (y + e_j, j) pulls S_j(y) when that neighbour is in range
+      Re v = P.valid(opp(j)) ? __ldg(nu + j * N + P.raw(opp(j))) : Re(0);
+      // (b) output (y, j) keeps S_j(y) when its own source is out of range
+      if (!P.valid(j)) v += __ldg(nu + j * N + idx);
+      mu[j] = v;
+    }
+
+    // ---- f_k (recompute) --------------------------------------------------
+    Re f[Q];
+    if (A.first) {
+      const Re* f0 = static_cast<const Re*>(a.src);
+#pragma unroll
+      for (int i = 0; i < Q; ++i) f[i] = __ldg(f0 + i * N + idx);
+    } else {
+      pull_post_bc<St>(a, static_cast<const St*>(a.src), idx, x, y, z, tag, f);
+    }
+
+    // ---- boundary-cell corrections of T^T, force seed --------------------
+    if (ri) {
+      const LinkRec& r = a.rec[ri - 1];
+      const uint32_t lm = r.linkmask, nbw = r.nb_wall, nbl = r.nb_low;
+#pragma unroll
+      for (int j = 1; j < Q; ++j) {
+        // own output j is a wall output: no normal / fallback term
+        const bool wall_out = (lm >> opp(j)) & 1u;
+        const bool a_ok = P.valid(opp(j)) && !((nbw >> j) & 1u);
+        Re v = a_ok ? __ldg(nu + j * N + P.raw(opp(j))) : Re(0);
+        if (!P.valid(j) && !wall_out) v += __ldg(nu + j * N + idx);
+        if ((nbl >> j) & 1u) {
+          const int w = ahead_wrap(g, x, y, z, ex(j), ey(j), ez(j));
+          v += (Re(1) - Re(2) * Re(r.qnb[j])) * __ldg(nu + opp(j) * N + w);
+        }
+        mu[j] = v;
+      }
+#pragma unroll
+      for (int i = 1; i < Q; ++i) {
+        const int io = opp(i);
+        if ((lm >> io) & 1u) {
+          const Re qv = Re(r.q[io]);
+          const Re nv = __ldg(nu + i * N + idx);
+          if (qv >= Re(0.5)) {
+            const Re a2 = Re(1) / (Re(2) * fmin(qv, Re(1)));
+            mu[io] += a2 * nv;
+            mu[i] += (Re(1) - a2) * nv;
+          } else {
+            mu[io] += Re(2) * fmax(qv, Re(0)) * nv;
+          }
+        }
+      }
+      if (A.last) {
+        const Re gfx = Re(*A.dj_dfx);
+#pragma unroll
+        for (int j = 1; j < Q; ++j)
+          if (ex(j) != 0 && ((lm >> j) & 1u)) mu[j] += Re(ex(j)) * gfx;
+      }
+    }
+
+    // ---- collide forward (needed by the porosity / q gradients) ----------
+    const bool soft = (fl & (SF_SOLID_SPHERE | SF_SOLID_FIELD)) != 0;
+    const bool hard = (fl & SF_SOLID_HARD) && (tag & TAG_SOLID);
+    Re p = Re(0), dpdr = Re(0);
+    if (soft) {
+      if (fl & SF_SOLID_SPHERE)
+        p = sphere_porosity<Re>(a.sph, x, y, z, &dpdr);
+      else
+        p = a.porosity[idx];
+    }
+    if (soft || ri) {
+      Re c[Q];
+      collide_cell<Re>(f, a.tau, MRT, (fl & SF_SMAG) != 0, a.c18cs2, a.K, c);
+      if (soft && (fl & SF_SOLID_SPHERE)) {
+        Re gp = Re(0);
+#pragma unroll
+        for (int i = 0; i < Q; ++i) gp += mu[i] * (c[opp(i)] - c[i]);
+        gr += double(gp) * double(dpdr);
+      }
+      if (ri) {
+        // dJ/dq of the links of y at this step: d T(S_k)/dq with S_k = B(c)
+        const LinkRec& r = a.rec[ri - 1];
+        const uint32_t lm = r.linkmask;
+        const St* Sk = static_cast<const St*>(A.S_k);
+        double* gq = A.gq + size_t(ri - 1) * Q;
+#pragma unroll
+        for (int i = 1; i < Q; ++i) {
+          const int io = opp(i);
+          if ((lm >> io) & 1u) {
+            const Re qv = Re(r.q[io]);
+            const Re nv = __ldg(A.nu_in + i * N + idx);
+            const Re s_io = soft ? (Re(1) - p) * c[io] + p * c[i] : (hard ? c[i] : c[io]);
+            Re dout;
+            if (qv >= Re(0.5)) {
+              const Re s_i = soft ? (Re(1) - p) * c[i] + p * c[io] : (hard ? c[io] : c[i]);
+              dout = (qv < Re(1)) ? -(s_io - s_i) / (Re(2) * qv * qv) : Re(0);
+            } else {
+              const int nb = ahead_wrap(g, x, y, z, ex(i), ey(i), ez(i));
+              const Re s_nb = S::ld(Sk + io * N + nb, a.K.w[io]);
+              dout = (qv > Re(0)) ? Re(2) * (s_io - s_nb) : Re(0);
+            }
+            const double gqv = double(nv) * double(dout);
+            gq[io] += gqv;
+            gr += gqv * r.dqdr[io];
+          }
+        }
+      }
+    }
+
+    // ---- B^T -------------------------------------------------------------
+    if (soft) {
+      Re m2[Q];
+#pragma unroll
+      for (int i = 0; i < Q; ++i) m2[i] = (Re(1) - p) * mu[i] + p * mu[opp(i)];
+#pragma unroll
+      for (int i = 0; i < Q; ++i) mu[i] = m2[i];
+    } else if (hard) {
+      Re m2[Q];
+#pragma unroll
+      for (int i = 0; i < Q; ++i) m2[i] = mu[opp(i)];
+#pragma unroll
+      for (int i = 0; i < Q; ++i) mu[i] = m2[i];
+    }
+
+    // ---- lambda_k = C^T mu ------------------------------------------------
+    Re lam[Q];
+    collide_vjp<Re>(f, mu, a.tau, MRT, (fl & SF_SMAG) != 0, a.c18cs2, a.K, lam, nullptr);
+
+    // ---- nu_k = Z^T lambda_k on the faces ---------------------------------
+    if (!A.first) {
+      if (x == g.nx - 1 && !(fl & SF_NO_OUTLET)) zou_he_outlet_T<Re>(lam, a.rho_out);
+      if (x == 0 && !(fl & SF_NO_INLET)) {
+        Re ux = a.u_in[0], uy = a.u_in[1], uz = a.u_in[2];
+        if (fl & SF_INLET_FACE) {
+          const int fi = y * g.nz + z, fn = g.ny * g.nz;
+          ux = a.u_face[fi];
+          uy = a.u_face[fn + fi];
+          uz = a.u_face[2 * fn + fi];
+        }
+        zou_he_inlet_T<Re>(lam, ux, uy, uz);
+      }
+    }
+#pragma unroll
+    for (int i = 0; i < Q; ++i) A.nu_out[i * N + idx] = lam[i];
+  }
+
+  // deterministic per-block accumulation of dJ/dr across steps
+  __shared__ double sh[32];
+#pragma unroll
+  for (int o = 16; o > 0; o >>= 1) gr += __shfl_down_sync(0xffffffffu, gr, o);
+  const int lane = threadIdx.x & 31, wid = threadIdx.x >> 5;
+  if (lane == 0) sh[wid] = gr;
+  __syncthreads();
+  if (wid == 0) {
+    const int nw = (blockDim.x + 31) >> 5;
+    gr = lane < nw ? sh[lane] : 0.0;
+#pragma unroll
+    for (int o = 16; o > 0; o >>= 1) gr += __shfl_down_sync(0xffffffffu, gr, o);
+    if (lane == 0) A.gr_partials[blockIdx.x] += gr;
+  }
+}
+
+// nu_N = Z^T lambda_N with lambda_N = dJ/df_N from the momentum exchange:
+// lambda_N[opp j](x) = dJ/dFx * e_jx on every link (x, j).
+template <class Re>
+__global__ void k_adjoint_seed(StepArgs<Re> a, const double* __restrict__ dj_dfx,
+                               Re* __restrict__ nu) {
+  const Grid& g = a.g;
+  const int idx = blockIdx.x * blockDim.x + threadIdx.x;
+  if (idx >= g.n) return;
+  const size_t N = size_t(g.n);
+  Re l[Q];
+#pragma unroll
+  for (int i = 0; i < Q; ++i) l[i] = Re(0);
+  const uint32_t tag = a.tag ? a.tag[idx] : 0u;
+  const uint32_t ri = tag & TAG_INDEX;
+  if (ri) {
+    const uint32_t lm = a.rec[ri - 1].linkmask;
+    const Re gfx = Re(*dj_dfx);
+#pragma unroll
+    for (int j = 1; j < Q; ++j)
+      if (ex(j) != 0 && ((lm >> j) & 1u)) l[opp(j)] += Re(ex(j)) * gfx;
+    const int z = idx % g.nz, t = idx / g.nz, y = t % g.ny, x = t / g.ny;
+    if (x == g.nx - 1 && !(a.flags & SF_NO_OUTLET)) zou_he_outlet_T<Re>(l, a.rho_out);
+    if (x == 0 && !(a.flags & SF_NO_INLET)) {
+      Re ux = a.u_in[0], uy = a.u_in[1], uz = a.u_in[2];
+      if (a.flags & SF_INLET_FACE) {
+        const int fi = y * g.nz + z, fn = g.ny * g.nz;
+        ux = a.u_face[fi];
+        uy = a.u_face[fn + fi];
+        uz = a.u_face[2 * fn + fi];
+      }
+      zou_he_inlet_T<Re>(l, ux, uy, uz);
+    }
+  }
+#pragma unroll
+  for (int i = 0; i < Q; ++i) nu[i * N + idx] = l[i];
+}
+
+// dJ/dFx = sign(Fx) / (0.5 rho U^2 A + 1e-10) from the finalized force record
+// out = (Fx, Fy, Fz, Cd).
+__global__ void k_dj_dfx(const double* __restrict__ fcd, double dyn_area, double* __restrict__ g) {
+  const double fx = fcd[0];
+  const double s = fx > 0.0 ? 1.0 : (fx < 0.0 ? -1.0 : 0.0);
+  *g = s / (dyn_area + 1e-10);
+}
+
+// per-block partials -> scalar (fixed order)
+__global__ void k_reduce_sum(const double* __restrict__ part, int n, double* __restrict__ out) {
+  __shared__ double sh[256];
+  double s = 0.0;
+  for (int i = threadIdx.x; i < n; i += blockDim.x) s += part[i];
+  sh[threadIdx.x] = s;
+  __syncthreads();
+  for (int o = blockDim.x / 2; o > 0; o >>= 1) {
+    if (threadIdx.x < o) sh[threadIdx.x] += sh[threadIdx.x + o];
+    __syncthreads();
+  }
+  if (threadIdx.x == 0) *out = sh[0];
+}
+
+// per-link dJ/dq -> dense [19][n] (zero where there is no link)
+template <class Re>
+__global__ void k_scatter_gq(Grid g, const uint32_t* __restrict__ tag,
+                             const LinkRec* __restrict__ rec, const double* __restrict__ gq,
+                             Re* __restrict__ out) {
+  const int idx = blockIdx.x * blockDim.x + threadIdx.x;
+  if (idx >= g.n) return;
+  const size_t N = size_t(g.n);
+  const uint32_t ri = tag[idx] & TAG_INDEX;
+  uint32_t lm = ri ? rec[ri - 1].linkmask : 0u;
+#pragma unroll
+  for (int j = 0; j < Q; ++j)
+    out[j * N + idx] = ((lm >> j) & 1u) ? Re(gq[size_t(ri - 1) * Q + j]) : Re(0);
+}
+
+static inline int nblk(int n) { return (n + 255) / 256; }
+
+template <class St>
+cudaError_t launch_adjoint(const AdjArgs<typename Storage<St>::Re>& A, bool mrt,
+                           cudaStream_t st) {
+  if (mrt)
+    k_adjoint<St, true><<<nblk(A.s.g.n), 256, 0, st>>>(A);
+  else
+    k_adjoint<St, false><<<nblk(A.s.g.n), 256, 0, st>>>(A);
+  return cudaGetLastError();
+}
+
+template <class Re>
+cudaError_t launch_adjoint_seed(const StepArgs<Re>& a, const double* dj, Re* nu, cudaStream_t st) {
+  k_adjoint_seed<Re><<<nblk(a.g.n), 256, 0, st>>>(a, dj, nu);
+  return cudaGetLastError();
+}
+
+cudaError_t launch_dj_dfx(const double* fcd, double dyn_area, double* g, cudaStream_t st) {
+  k_dj_dfx<<<1, 1, 0, st>>>(fcd, dyn_area, g);
+  return cudaGetLastError();
+}
+
+cudaError_t launch_reduce_sum(const double* part, int n, double* out, cudaStream_t st) {
+  k_reduce_sum<<<1, 256, 0, st>>>(part, n, out);
+  return cudaGetLastError();
+}
+
+template <class Re>
+cudaError_t launch_scatter_gq(const Grid& g, const uint32_t* tag, const LinkRec* rec,
+                              const double* gq, Re* out, cudaStream_t st) {
+  k_scatter_gq<Re><<<nblk(g.n), 256, 0, st>>>(g, tag, rec, gq, out);
+  return cudaGetLastError();
+}
+
+template cudaError_t launch_adjoint<float>(const AdjArgs<float>&, bool, cudaStream_t);
+template cudaError_t launch_adjoint<double>(const AdjArgs<double>&, bool, cudaStream_t);
+template cudaError_t launch_adjoint<__half>(const AdjArgs<float>&, bool, cudaStream_t);
+template cudaError_t launch_adjoint<__nv_bfloat16>(const AdjArgs<float>&, bool, cudaStream_t);
+template cudaError_t launch_adjoint_seed<float>(const StepArgs<float>&, const double*, float*,
+                                                cudaStream_t);
+template cudaError_t launch_adjoint_seed<double>(const StepArgs<double>&, const double*, double*,
+                                                 cudaStream_t);
+template cudaError_t launch_scatter_gq<float>(const Grid&, const uint32_t*, const LinkRec*,
+                                              const double*, float*, cudaStream_t);
+template cudaError_t launch_scatter_gq<double>(const Grid&, const uint32_t*, const LinkRec*,
+                                               const double*, double*, cudaStream_t);
+
+}  // namespace lbm

@@ -38,6 +38,27 @@ cudaError_t launch_classify(const Grid& g, const uint8_t* solid, const Re* q, co
                             cudaStream_t st);
 cudaError_t launch_area_cols(const Grid& g, const uint8_t* solid, int* col, cudaStream_t st);
 
+template <class Re> struct AdjArgs {
+  StepArgs<Re> s;
+  const void* S_k;
+  const Re* nu_in;
+  Re* nu_out;
+  int first;
+  int last;
+  const double* dj_dfx;
+  double* gr_partials;
+  double* gq;
+};
+template <class St>
+cudaError_t launch_adjoint(const AdjArgs<typename Storage<St>::Re>& A, bool mrt, cudaStream_t st);
+template <class Re>
+cudaError_t launch_adjoint_seed(const StepArgs<Re>& a, const double* dj, Re* nu, cudaStream_t st);
+cudaError_t launch_dj_dfx(const double* fcd, double dyn_area, double* g, cudaStream_t st);
+cudaError_t launch_reduce_sum(const double* part, int n, double* out, cudaStream_t st);
+template <class Re>
+cudaError_t launch_scatter_gq(const Grid& g, const uint32_t* tag, const LinkRec* rec,
+                              const double* gq, Re* out, cudaStream_t st);
+
 }  // namespace lbm
 
 using namespace lbm;
@@ -67,6 +88,14 @@ struct lbm_sim {
   double* partials = nullptr;
   int nblocks = 0;
   unsigned long long* guard_count = nullptr;
+  // adjoint workspace (grown on demand, kept between calls)
+  void* states = nullptr;    // checkpoints + stash, storage dtype
+  size_t states_cap = 0;     // in states
+  void* nu[2] = {nullptr, nullptr};
+  double* gq = nullptr;
+  int gq_cap = 0;
+  double* gr_partials = nullptr;
+  double* scal = nullptr;    // [0..3] F, Cd ; [4] dJ/dFx ; [5] dJ/dr
 };
 
 namespace {
@@ -154,6 +183,59 @@ int launch(const lbm_sim* s, const void* src, void* dst, int extra_flags, cudaSt
     }
   }
   return cuda_check(e, "k_step launch");
+}
+
+template <class Re>
+int adjoint_launch_t(const lbm_sim* s, const void* S_prev, const void* S_k, const Re* nu_in,
+                     Re* nu_out, int first, int last, cudaStream_t st) {
+  AdjArgs<Re> A;
+  memset(&A, 0, sizeof(A));
+  fill_args<Re>(s, A.s);
+  A.s.flags &= ~(SF_GUARD_PRE | SF_GUARD_POST);
+  A.s.src = S_prev;
+  A.S_k = S_k;
+  A.nu_in = nu_in;
+  A.nu_out = nu_out;
+  A.first = first;
+  A.last = last;
+  A.dj_dfx = s->scal + 4;
+  A.gr_partials = s->gr_partials;
+  A.gq = s->gq;
+  const bool mrt = s->p.collision == LBM_MRT;
+  cudaError_t e;
+  if constexpr (sizeof(Re) == 8) {
+    e = launch_adjoint<double>(A, mrt, st);
+  } else {
+    switch (s->p.storage) {
+      case LBM_F32: e = launch_adjoint<float>(A, mrt, st); break;
+      case LBM_F16: e = launch_adjoint<__half>(A, mrt, st); break;
+      default: e = launch_adjoint<__nv_bfloat16>(A, mrt, st); break;
+    }
+  }
+  return cuda_check(e, "k_adjoint launch");
+}
+
+int adjoint_launch(const lbm_sim* s, const void* S_prev, const void* S_k, const void* nu_in,
+                   void* nu_out, int first, int last, cudaStream_t st) {
+  if (is_fp64(s))
+    return adjoint_launch_t<double>(s, S_prev, S_k, static_cast<const double*>(nu_in),
+                                    static_cast<double*>(nu_out), first, last, st);
+  return adjoint_launch_t<float>(s, S_prev, S_k, static_cast<const float*>(nu_in),
+                                 static_cast<float*>(nu_out), first, last, st);
+}
+
+int adjoint_seed(const lbm_sim* s, void* nu, cudaStream_t st) {
+  cudaError_t e;
+  if (is_fp64(s)) {
+    StepArgs<double> a;
+    fill_args<double>(s, a);
+    e = launch_adjoint_seed<double>(a, s->scal + 4, static_cast<double*>(nu), st);
+  } else {
+    StepArgs<float> a;
+    fill_args<float>(s, a);
+    e = launch_adjoint_seed<float>(a, s->scal + 4, static_cast<float*>(nu), st);
+  }
+  return cuda_check(e, "adjoint seed");
 }
 
 double dyn_area(const lbm_sim* s) {
@@ -341,6 +423,12 @@ int lbm_destroy(lbm_sim* s) {
   cudaFree(s->partials);
   cudaFree(s->guard_count);
   cudaFree(s->u_face);
+  cudaFree(s->states);
+  cudaFree(s->nu[0]);
+  cudaFree(s->nu[1]);
+  cudaFree(s->gq);
+  cudaFree(s->gr_partials);
+  cudaFree(s->scal);
   free_geometry(s);
   delete s;
   return LBM_OK;
@@ -462,6 +550,107 @@ int lbm_run(lbm_sim* s, int n_steps, int sample_every, double* samples, void* st
     LBM_TRY(cuda_check(launch_force_finalize(s->partials, s->nblocks, da, samples + 4 * si, st),
                        "force finalize"));
   }
+  return LBM_OK;
+}
+
+int lbm_cd_and_grad(lbm_sim* s, int n_steps, int checkpoint_every, double* cd_host,
+                    double* dcd_dr_host, void* dcd_dq, void* dcd_df0, void* stream) {
+  if (!s || !cd_host || !dcd_dr_host) return set_error(LBM_ERR_ARG, "lbm_cd_and_grad: null argument");
+  if (n_steps < 1) return set_error(LBM_ERR_ARG, "lbm_cd_and_grad: n_steps < 1");
+  if (!s->have_geometry) return set_error(LBM_ERR_STATE, "lbm_cd_and_grad: set a geometry first");
+  if (s->state_is_S)
+    return set_error(LBM_ERR_STATE, "lbm_cd_and_grad: needs the initial state; call lbm_set_state");
+  if (s->p.guard != LBM_GUARD_OFF)
+    return set_error(LBM_ERR_UNSUPPORTED,
+                     "lbm_cd_and_grad: the stability guard is not differentiated (the reference "
+                     "gradient drivers run without it)");
+  LBM_TRY(check_align(dcd_dq, s->re_bytes, "dcd_dq"));
+  LBM_TRY(check_align(dcd_df0, s->re_bytes, "dcd_df0"));
+  cudaStream_t st = static_cast<cudaStream_t>(stream);
+  const int N = n_steps;
+  int K = checkpoint_every <= 0 ? N : checkpoint_every;
+  if (K > N) K = N;
+  const int nseg = (N + K - 1) / K;
+  const size_t state_bytes = s->n * Q * s->st_bytes;
+  const size_t need = size_t(nseg - 1) + size_t(K + 1);
+  if (s->states_cap < need) {
+    cudaFree(s->states);
+    s->states = nullptr;
+    s->states_cap = 0;
+    LBM_TRY(dev_alloc(&s->states, need * state_bytes));
+    s->states_cap = need;
+  }
+  for (int b = 0; b < 2; ++b)
+    if (!s->nu[b]) LBM_TRY(dev_alloc(&s->nu[b], s->n * Q * s->re_bytes));
+  if (!s->gr_partials) LBM_TRY(dev_alloc((void**)&s->gr_partials, size_t(s->nblocks) * sizeof(double)));
+  if (!s->scal) LBM_TRY(dev_alloc((void**)&s->scal, 8 * sizeof(double)));
+  if (s->gq_cap < s->nrec) {
+    cudaFree(s->gq);
+    s->gq = nullptr;
+    s->gq_cap = 0;
+    LBM_TRY(dev_alloc((void**)&s->gq, size_t(s->nrec > 0 ? s->nrec : 1) * Q * sizeof(double)));
+    s->gq_cap = s->nrec;
+  }
+  char* base = static_cast<char*>(s->states);
+  auto ckpt = [&](int c) -> void* { return base + size_t(c) * state_bytes; };  // S_{(c+1)K-1}
+  auto stash = [&](int j) -> void* { return base + size_t(nseg - 1 + j) * state_bytes; };
+  const int a_last = (nseg - 1) * K;
+
+  // ---- forward: checkpoints at segment starts, last segment straight into the stash
+  const void* prev = s->fbuf;
+  for (int k = 0; k < N; ++k) {
+    void* dst;
+    if (k >= a_last)
+      dst = stash(k - a_last + 1);
+    else if ((k + 1) % K == 0)
+      dst = ckpt((k + 1) / K - 1);
+    else
+      dst = s->S[k & 1];
+    LBM_TRY(launch(s, prev, dst, k == 0 ? SF_COLLIDE_ONLY : 0, st));
+    prev = dst;
+  }
+  LBM_TRY(launch(s, prev, s->nu[1], SF_STREAM_ONLY | SF_FORCE, st));
+  LBM_TRY(cuda_check(launch_force_finalize(s->partials, s->nblocks, dyn_area(s), s->scal, st), "force"));
+  LBM_TRY(cuda_check(launch_dj_dfx(s->scal, dyn_area(s), s->scal + 4, st), "dJ/dFx"));
+
+  // ---- backward
+  LBM_TRY(cuda_check(cudaMemsetAsync(s->gr_partials, 0, size_t(s->nblocks) * sizeof(double), st), "memset"));
+  LBM_TRY(cuda_check(cudaMemsetAsync(s->gq, 0, size_t(s->gq_cap > 0 ? s->gq_cap : 1) * Q * sizeof(double), st), "memset"));
+  int cur = 0;
+  LBM_TRY(adjoint_seed(s, s->nu[cur], st));
+  for (int c = nseg - 1; c >= 0; --c) {
+    const int a0 = c * K, b0 = (a0 + K < N) ? a0 + K : N;
+    const void* slot0 = a0 == 0 ? s->fbuf : ckpt(c - 1);
+    if (c != nseg - 1) {
+      const void* pv = slot0;
+      for (int k = a0; k < b0; ++k) {
+        void* dst = stash(k - a0 + 1);
+        LBM_TRY(launch(s, pv, dst, k == 0 ? SF_COLLIDE_ONLY : 0, st));
+        pv = dst;
+      }
+    }
+    for (int k = b0 - 1; k >= a0; --k) {
+      const void* Sprev = (k == a0) ? slot0 : stash(k - a0);
+      LBM_TRY(adjoint_launch(s, Sprev, stash(k - a0 + 1), s->nu[cur], s->nu[1 - cur], k == 0,
+                             k == N - 1, st));
+      cur = 1 - cur;
+    }
+  }
+  LBM_TRY(cuda_check(launch_reduce_sum(s->gr_partials, s->nblocks, s->scal + 5, st), "reduce"));
+  if (dcd_dq) {
+    cudaError_t e = is_fp64(s)
+        ? launch_scatter_gq<double>(s->g, s->tag, s->rec, s->gq, static_cast<double*>(dcd_dq), st)
+        : launch_scatter_gq<float>(s->g, s->tag, s->rec, s->gq, static_cast<float*>(dcd_dq), st);
+    LBM_TRY(cuda_check(e, "scatter dq"));
+  }
+  if (dcd_df0)
+    LBM_TRY(cuda_check(cudaMemcpyAsync(dcd_df0, s->nu[cur], s->n * Q * s->re_bytes,
+                                       cudaMemcpyDeviceToDevice, st), "df0 copy"));
+  double h[8];
+  LBM_TRY(cuda_check(cudaMemcpyAsync(h, s->scal, 8 * sizeof(double), cudaMemcpyDeviceToHost, st), "D2H"));
+  LBM_TRY(cuda_check(cudaStreamSynchronize(st), "sync"));
+  *cd_host = h[3];
+  *dcd_dr_host = h[5];
   return LBM_OK;
 }
 

@@ -346,17 +346,54 @@ __host__ __device__ __forceinline__ void raw_second_moments(const Re f[Q], Re p[
   p[5] = (f[15] + f[18]) - (f[16] + f[17]);    // sum ey ez f
 }
 
-// Non-equilibrium stress from raw second moments p and (rho, u).
+// Second moments of f_eq in closed form, exact for any symmetric weight set:
+// sum_i e_ia e_ib feq_i = rho [W2 (1 - 1.5 u^2) + 4.5 (W2 u_a^2 + W22 (u^2 - u_a^2))] (a = b)
+//                       = 9 W22 rho u_a u_b                                    (a != b)
+// with W2 = sum_i w_i e_ix^2 = 2 w_face + 8 w_edge and W22 = sum_i w_i e_ix^2 e_iy^2
+// = 4 w_edge (1/3 and 1/9 for the rational weights; the float32-rounded
+// weights of lattice.py:53-60 shift them by ~1e-8, which this form keeps).
 template <class Re>
-__host__ __device__ __forceinline__ void neq_stress(const Re p[6], Re rho, Re ux, Re uy, Re uz,
-                                                    Re s[6]) {
-  const Re r3 = rho * Re(1.0 / 3.0);
-  s[0] = p[0] - (r3 + rho * ux * ux);
-  s[1] = p[1] - (r3 + rho * uy * uy);
-  s[2] = p[2] - (r3 + rho * uz * uz);
-  s[3] = p[3] - rho * ux * uy;
-  s[4] = p[4] - rho * ux * uz;
-  s[5] = p[5] - rho * uy * uz;
+__host__ __device__ __forceinline__ void eq_second(const Re w[Q], Re rho, Re ux, Re uy, Re uz,
+                                                   Re e[6]) {
+  const Re W2 = Re(2) * w[1] + Re(8) * w[7], W22 = Re(4) * w[7];
+  const Re xx = ux * ux, yy = uy * uy, zz = uz * uz;
+  const Re base = W2 * (Re(1) - Re(1.5) * (xx + yy + zz));
+  e[0] = rho * (base + Re(4.5) * (W2 * xx + W22 * (yy + zz)));
+  e[1] = rho * (base + Re(4.5) * (W2 * yy + W22 * (xx + zz)));
+  e[2] = rho * (base + Re(4.5) * (W2 * zz + W22 * (xx + yy)));
+  const Re c9 = Re(9) * W22 * rho;
+  e[3] = c9 * ux * uy;
+  e[4] = c9 * ux * uz;
+  e[5] = c9 * uy * uz;
+}
+
+// Cotangent ge on eq_second -> (g_rho, g_u).
+template <class Re>
+__host__ __device__ __forceinline__ void eq_second_vjp(const Re w[Q], Re rho, Re ux, Re uy,
+                                                       Re uz, const Re ge[6], Re& gr, Re& gx,
+                                                       Re& gy, Re& gz) {
+  const Re W2 = Re(2) * w[1] + Re(8) * w[7], W22 = Re(4) * w[7];
+  const Re xx = ux * ux, yy = uy * uy, zz = uz * uz;
+  const Re base = W2 * (Re(1) - Re(1.5) * (xx + yy + zz));
+  const Re c9 = Re(9) * W22;
+  gr = ge[0] * (base + Re(4.5) * (W2 * xx + W22 * (yy + zz))) +
+       ge[1] * (base + Re(4.5) * (W2 * yy + W22 * (xx + zz))) +
+       ge[2] * (base + Re(4.5) * (W2 * zz + W22 * (xx + yy))) +
+       c9 * (ge[3] * ux * uy + ge[4] * ux * uz + ge[5] * uy * uz);
+  const Re own = Re(6) * W2, oth = Re(9) * W22 - Re(3) * W2;
+  gx = rho * (ux * (own * ge[0] + oth * (ge[1] + ge[2])) + c9 * (ge[3] * uy + ge[4] * uz));
+  gy = rho * (uy * (own * ge[1] + oth * (ge[0] + ge[2])) + c9 * (ge[3] * ux + ge[5] * uz));
+  gz = rho * (uz * (own * ge[2] + oth * (ge[0] + ge[1])) + c9 * (ge[4] * ux + ge[5] * uy));
+}
+
+// Non-equilibrium stress Pi_ab = sum_i e_ia e_ib f_i - sum_i e_ia e_ib feq_i.
+template <class Re>
+__host__ __device__ __forceinline__ void neq_stress(const Re p[6], const Re w[Q], Re rho, Re ux,
+                                                    Re uy, Re uz, Re s[6]) {
+  Re e[6];
+  eq_second<Re>(w, rho, ux, uy, uz, e);
+#pragma unroll
+  for (int k = 0; k < 6; ++k) s[k] = p[k] - e[k];
 }
 
 template <class Re>
@@ -430,7 +467,7 @@ __host__ __device__ __forceinline__ Re collide_cell_rj(const Re f[Q], Re rho, Re
       // raw second moments from the MRT partial sums: sum ex^2 f = (m0 + ... )
       Re p[6], s[6];
       raw_second_moments<Re>(f, p);
-      neq_stress<Re>(p, rho, ux, uy, uz, s);
+      neq_stress<Re>(p, K.w, rho, ux, uy, uz, s);
       omega = Re(1) / smag_tau<Re>(tau, c18cs2, smag_pi<Re>(s), inv_rho_eps<Re>(rho, ir));
     } else {
       omega = Re(1) / tau;
@@ -440,7 +477,7 @@ __host__ __device__ __forceinline__ Re collide_cell_rj(const Re f[Q], Re rho, Re
     if (smag) {
       Re p[6], s[6];
       raw_second_moments<Re>(f, p);
-      neq_stress<Re>(p, rho, ux, uy, uz, s);
+      neq_stress<Re>(p, K.w, rho, ux, uy, uz, s);
       omega = Re(1) / smag_tau<Re>(tau, c18cs2, smag_pi<Re>(s), inv_rho_eps<Re>(rho, ir));
     } else {
       omega = Re(1) / tau;
@@ -481,7 +518,7 @@ __host__ __device__ __forceinline__ void collide_vjp(const Re f[Q], const Re lam
   if (smag) {
     Re p[6];
     raw_second_moments<Re>(f, p);
-    neq_stress<Re>(p, rho, ux, uy, uz, sst);
+    neq_stress<Re>(p, K.w, rho, ux, uy, uz, sst);
     pi = smag_pi<Re>(sst);
     inv_rr = inv_rho_eps<Re>(rho, ir);
     R = sqrt(tau * tau + c18cs2 * pi * inv_rr);
@@ -545,27 +582,29 @@ __host__ __device__ __forceinline__ void collide_vjp(const Re f[Q], const Re lam
     if (pi > Re(0)) {
       // d pi / d s (s = xx, yy, zz, xy, xz, yz; off-diagonals counted twice)
       const Re ip = g_pi / pi;
-      const Re gs0 = ip * sst[0], gs1 = ip * sst[1], gs2 = ip * sst[2];
-      const Re gs3 = Re(2) * ip * sst[3], gs4 = Re(2) * ip * sst[4], gs5 = Re(2) * ip * sst[5];
-      // s_ab = p_ab(f) - rho/3 delta_ab - j_a j_b / rho
-      const Re t2 = -(gs0 + gs1 + gs2) * Re(1.0 / 3.0) +
-                    (gs0 * ux * ux + gs1 * uy * uy + gs2 * uz * uz + gs3 * ux * uy +
-                     gs4 * ux * uz + gs5 * uy * uz);
-      const Re bx = Re(2) * gs0 * ux + gs3 * uy + gs4 * uz;
-      const Re by = Re(2) * gs1 * uy + gs3 * ux + gs5 * uz;
-      const Re bz = Re(2) * gs2 * uz + gs4 * ux + gs5 * uy;
+      Re gs[6];
+      gs[0] = ip * sst[0];
+      gs[1] = ip * sst[1];
+      gs[2] = ip * sst[2];
+      gs[3] = Re(2) * ip * sst[3];
+      gs[4] = Re(2) * ip * sst[4];
+      gs[5] = Re(2) * ip * sst[5];
+      // s = p(f) - eq(rho, u): direct part through the raw moments p
 #pragma unroll
       for (int i = 0; i < Q; ++i) {
         const int x = ex(i), y = ey(i), z = ez(i);
-        Re t = t2;
-        if (x != 0) t += gs0 - Re(x) * bx;
-        if (y != 0) t += gs1 - Re(y) * by;
-        if (z != 0) t += gs2 - Re(z) * bz;
-        if (x * y != 0) t += Re(x * y) * gs3;
-        if (x * z != 0) t += Re(x * z) * gs4;
-        if (y * z != 0) t += Re(y * z) * gs5;
+        Re t = Re(0);
+        if (x != 0) t += gs[0];
+        if (y != 0) t += gs[1];
+        if (z != 0) t += gs[2];
+        if (x * y != 0) t += Re(x * y) * gs[3];
+        if (x * z != 0) t += Re(x * z) * gs[4];
+        if (y * z != 0) t += Re(y * z) * gs[5];
         gf[i] += t;
       }
+      Re er, exx, eyy, ezz;
+      eq_second_vjp<Re>(K.w, rho, ux, uy, uz, gs, er, exx, eyy, ezz);
+      macro_vjp_add<Re>(-er, -exx, -eyy, -ezz, rho, ux, uy, uz, gf);
     }
 #pragma unroll
     for (int i = 0; i < Q; ++i) gf[i] += g_rho_direct;

@@ -152,6 +152,99 @@ __device__ __forceinline__ bool unstable_rj(Re rho, Re jx, Re jy, Re jz) {
   return (rho < Re(0.3)) || (rho > Re(2.0)) || (um > Re(0.4)) || (rho != rho);
 }
 
+// Pull offsets of one cell, hoisted out of the 19-direction loop: source
+// coordinate s = x - e along each axis, with validity (x never periodic;
+// y/z periodic or clamped, streaming.py:109-142).
+struct PullIdx {
+  int xo[3], yo[3], zo[3];   // index 0: e = -1, 1: e = 0, 2: e = +1
+  bool xv[3], yv[3], zv[3];
+  __device__ __forceinline__ PullIdx(const Grid& g, int x, int y, int z) {
+    const int nyz = g.ny * g.nz;
+    xo[0] = (x + 1) * nyz; xo[1] = x * nyz; xo[2] = (x - 1) * nyz;
+    xv[0] = x < g.nx - 1; xv[1] = true; xv[2] = x > 0;
+    int yp = y + 1, ym = y - 1, zp = z + 1, zm = z - 1;
+    if (g.periodic_yz) {
+      yp = yp >= g.ny ? yp - g.ny : yp;
+      ym = ym < 0 ? ym + g.ny : ym;
+      zp = zp >= g.nz ? zp - g.nz : zp;
+      zm = zm < 0 ? zm + g.nz : zm;
+      yv[0] = yv[2] = zv[0] = zv[2] = true;
+    } else {
+      yv[0] = y < g.ny - 1; yv[2] = y > 0;
+      zv[0] = z < g.nz - 1; zv[2] = z > 0;
+    }
+    yv[1] = zv[1] = true;
+    yo[0] = yp * g.nz; yo[1] = y * g.nz; yo[2] = ym * g.nz;
+    zo[0] = zp; zo[1] = z; zo[2] = zm;
+  }
+  __device__ __forceinline__ int src(int i, int idx) const {
+    const int a = 1 + ex(i), b = 1 + ey(i), c = 1 + ez(i);
+    const bool ok = xv[a] && yv[b] && zv[c];
+    return ok ? xo[a] + yo[b] + zo[c] : idx;
+  }
+  // forward pull of direction i reads (x - e_i) (no fallback)
+  __device__ __forceinline__ bool valid(int i) const {
+    return xv[1 + ex(i)] && yv[1 + ey(i)] && zv[1 + ez(i)];
+  }
+  __device__ __forceinline__ int raw(int i) const {
+    return xo[1 + ex(i)] + yo[1 + ey(i)] + zo[1 + ez(i)];
+  }
+};
+
+// Post-stream, post-boundary populations f_k of cell (x,y,z) from the stored
+// post-collision populations S_{k-1}: pull (streaming.py:109-142), Bouzidi on
+// the cell's wall links (streaming.py:148-183), Zou-He inlet/outlet
+// (boundary.py:35-200).
+template <class St>
+__device__ __forceinline__ void pull_post_bc(const StepArgs<typename Storage<St>::Re>& a,
+                                             const St* __restrict__ src, int idx, int x, int y,
+                                             int z, uint32_t tag,
+                                             typename Storage<St>::Re f[Q]) {
+  using Re = typename Storage<St>::Re;
+  using S = Storage<St>;
+  const Grid& g = a.g;
+  const size_t N = size_t(g.n);
+  {
+    const PullIdx P(g, x, y, z);
+#pragma unroll
+    for (int i = 0; i < Q; ++i) f[i] = S::ld(src + i * N + P.src(i, idx), a.K.w[i]);
+  }
+  const uint32_t ri = tag & TAG_INDEX;
+  if (ri) {
+    const LinkRec& r = a.rec[ri - 1];
+    const uint32_t lm = r.linkmask;
+#pragma unroll
+    for (int i = 1; i < Q; ++i) {
+      const int io = opp(i);
+      if (lm & (1u << io)) {
+        const Re qv = Re(r.q[io]);
+        const Re s_opp = S::ld(src + io * N + idx, a.K.w[io]);
+        if (qv >= Re(0.5)) {
+          const Re s_i = S::ld(src + i * N + idx, a.K.w[i]);
+          const Re inv2q = Re(1) / (Re(2) * fmin(qv, Re(1)));
+          f[i] = inv2q * s_opp + (Re(1) - inv2q) * s_i;
+        } else {
+          const int nb = ahead_wrap(g, x, y, z, ex(i), ey(i), ez(i));
+          const Re s_nb = S::ld(src + io * N + nb, a.K.w[io]);
+          const Re twoq = Re(2) * fmax(qv, Re(0));
+          f[i] = twoq * s_opp + (Re(1) - twoq) * s_nb;
+        }
+      }
+    }
+  }
+  if (x == 0 && !(a.flags & SF_NO_INLET)) {
+    Re ux = a.u_in[0], uy = a.u_in[1], uz = a.u_in[2];
+    if (a.flags & SF_INLET_FACE) {
+      const int fi = y * g.nz + z, fn = g.ny * g.nz;
+      ux = a.u_face[fi];
+      uy = a.u_face[fn + fi];
+      uz = a.u_face[2 * fn + fi];
+    }
+    zou_he_inlet<Re>(f, ux, uy, uz);
+  }
+  if (x == g.nx - 1 && !(a.flags & SF_NO_OUTLET)) zou_he_outlet<Re>(f, a.rho_out);
+}
+
 // Block-wide sum of three doubles; thread 0 writes them to out[blockIdx.x*3].
 __device__ __forceinline__ void block_sum3_store(double a, double b, double c, double* out) {
   __shared__ double sh[3][32];

@@ -19,38 +19,6 @@
 
 namespace lbm {
 
-// Pull offsets of one cell, hoisted out of the 19-direction loop: source
-// coordinate s = x - e along each axis, with validity (x never periodic;
-// y/z periodic or clamped, streaming.py:109-142).
-struct PullIdx {
-  int xo[3], yo[3], zo[3];   // index 0: e = -1, 1: e = 0, 2: e = +1
-  bool xv[3], yv[3], zv[3];
-  __device__ __forceinline__ PullIdx(const Grid& g, int x, int y, int z) {
-    const int nyz = g.ny * g.nz;
-    xo[0] = (x + 1) * nyz; xo[1] = x * nyz; xo[2] = (x - 1) * nyz;
-    xv[0] = x < g.nx - 1; xv[1] = true; xv[2] = x > 0;
-    int yp = y + 1, ym = y - 1, zp = z + 1, zm = z - 1;
-    if (g.periodic_yz) {
-      yp = yp >= g.ny ? yp - g.ny : yp;
-      ym = ym < 0 ? ym + g.ny : ym;
-      zp = zp >= g.nz ? zp - g.nz : zp;
-      zm = zm < 0 ? zm + g.nz : zm;
-      yv[0] = yv[2] = zv[0] = zv[2] = true;
-    } else {
-      yv[0] = y < g.ny - 1; yv[2] = y > 0;
-      zv[0] = z < g.nz - 1; zv[2] = z > 0;
-    }
-    yv[1] = zv[1] = true;
-    yo[0] = yp * g.nz; yo[1] = y * g.nz; yo[2] = ym * g.nz;
-    zo[0] = zp; zo[1] = z; zo[2] = zm;
-  }
-  __device__ __forceinline__ int src(int i, int idx) const {
-    const int a = 1 + ex(i), b = 1 + ey(i), c = 1 + ez(i);
-    const bool ok = xv[a] && yv[b] && zv[c];
-    return ok ? xo[a] + yo[b] + zo[c] : idx;
-  }
-};
-
 template <class St, bool MRT>
 __global__ void __launch_bounds__(256, sizeof(St) == 8 ? 2 : 4) k_step(const StepArgs<typename Storage<St>::Re> a) {
   using Re = typename Storage<St>::Re;
@@ -76,48 +44,7 @@ __global__ void __launch_bounds__(256, sizeof(St) == 8 ? 2 : 4) k_step(const Ste
 #pragma unroll
       for (int i = 0; i < Q; ++i) f[i] = __ldg(f0 + i * N + idx);
     } else {
-      const St* src = static_cast<const St*>(a.src);
-      {
-        const PullIdx P(g, x, y, z);
-#pragma unroll
-        for (int i = 0; i < Q; ++i) f[i] = S::ld(src + i * N + P.src(i, idx), a.K.w[i]);
-      }
-
-      const uint32_t ri = tag & TAG_INDEX;
-      if (ri) {
-        const LinkRec& r = a.rec[ri - 1];
-        const uint32_t lm = r.linkmask;
-#pragma unroll
-        for (int i = 1; i < Q; ++i) {
-          const int io = opp(i);
-          if (lm & (1u << io)) {
-            const Re qv = Re(r.q[io]);
-            const Re s_opp = S::ld(src + io * N + idx, a.K.w[io]);
-            if (qv >= Re(0.5)) {
-              const Re s_i = S::ld(src + i * N + idx, a.K.w[i]);
-              const Re inv2q = Re(1) / (Re(2) * fmin(qv, Re(1)));
-              f[i] = inv2q * s_opp + (Re(1) - inv2q) * s_i;
-            } else {
-              const int nb = ahead_wrap(g, x, y, z, ex(i), ey(i), ez(i));
-              const Re s_nb = S::ld(src + io * N + nb, a.K.w[io]);
-              const Re twoq = Re(2) * fmax(qv, Re(0));
-              f[i] = twoq * s_opp + (Re(1) - twoq) * s_nb;
-            }
-          }
-        }
-      }
-
-      if (x == 0 && !(fl & SF_NO_INLET)) {
-        Re ux = a.u_in[0], uy = a.u_in[1], uz = a.u_in[2];
-        if (fl & SF_INLET_FACE) {
-          const int fi = y * g.nz + z, fn = g.ny * g.nz;
-          ux = a.u_face[fi];
-          uy = a.u_face[fn + fi];
-          uz = a.u_face[2 * fn + fi];
-        }
-        zou_he_inlet<Re>(f, ux, uy, uz);
-      }
-      if (x == g.nx - 1 && !(fl & SF_NO_OUTLET)) zou_he_outlet<Re>(f, a.rho_out);
+      pull_post_bc<St>(a, static_cast<const St*>(a.src), idx, x, y, z, tag, f);
     }
 
     Re rho = density<Re>(f);

@@ -185,6 +185,31 @@ class Simulation:
         nat.call("lbm_run", self._h, n_steps, int(sample_every), _ptr(samples), _stream())
         return samples
 
+    def cd_and_grad(self, n_steps, checkpoint_every=0, dcd_dq=False, dcd_df0=False):
+        """Cd after n_steps from the state set by set_state, and dCd/dr.
+
+        The shape gradient flows through the ray-sphere q(r) (q_mode
+        "bouzidi") and the sigmoid porosity (porosity "soft"); with
+        q_mode "halfway" and porosity "hard" it is exactly 0.0, as in the
+        reference's halfway_hard mode.  checkpoint_every=K stores the
+        populations every K steps and recomputes in between (0: keep all).
+        Returns (cd, dcd_dr) or (cd, dcd_dr, extras) when dcd_dq / dcd_df0 are
+        requested (dense (19, nx, ny, nz) CUDA tensors).
+        """
+        cd, gr = ctypes.c_double(), ctypes.c_double()
+        extras = {}
+        dq = df0 = None
+        if dcd_dq:
+            dq = extras["dcd_dq"] = torch.empty((19,) + self.shape, dtype=self.dtype, device="cuda")
+        if dcd_df0:
+            df0 = extras["dcd_df0"] = torch.empty((19,) + self.shape, dtype=self.dtype,
+                                                  device="cuda")
+        nat.call("lbm_cd_and_grad", self._h, int(n_steps), int(checkpoint_every),
+                 ctypes.byref(cd), ctypes.byref(gr), _ptr(dq), _ptr(df0), _stream())
+        if extras:
+            return cd.value, gr.value, extras
+        return cd.value, gr.value
+
     # -- queries ------------------------------------------------------------
     @property
     def projected_area(self):

@@ -129,3 +129,29 @@ def cd_of_radius_bgk_f64(radius, nx=32, ny=16, nz=16, n_steps=10, u_inlet=0.05,
     area = max(ops.projected_area(solid), 1.0)
     cd, _ = cd_from(f_post, f, q, u_inlet, area)
     return cd
+
+
+def simulate_cd(radius, nx, ny, nz, n_steps, tau, u_inlet=0.05, q_mode="bouzidi",
+                porosity_mode="soft", sharpness=20.0, collision="mrt", smagorinsky_cs=None,
+                periodic_yz=True, center=(0.0, 0.0, 0.0), dtype=torch.float32,
+                disc_floor=1e-10, a_eps=1e-20, q_leaf=None, consts=None, return_parts=False):
+    """The reference gradient drivers' simulate_cd (examples/11:139-165,
+    examples/08:69-93): build the four-mode sphere from ``radius`` (a tensor
+    that may require grad), run n_steps of collide -> porosity blend ->
+    stream -> Zou-He, and return Cd from the final step.  ``q_leaf`` replaces
+    the q buffer (to differentiate with respect to q directly)."""
+    from .geometry import sphere_geometry
+    c = consts or ops.consts_for(dtype)
+    por, solid, q = sphere_geometry(nx, ny, nz, radius, q_mode, porosity_mode, sharpness, center,
+                                    dtype, disc_floor, a_eps)
+    if q_leaf is not None:
+        q = q_leaf
+    f = initial_state(nx, ny, nz, u_inlet, dtype, c)
+    cfg = StepConfig(tau=tau, inlet=(u_inlet, 0.0, 0.0), collision=collision,
+                     smagorinsky_cs=smagorinsky_cs, periodic_yz=periodic_yz)
+    f, f_post, _ = run(f, q, cfg, n_steps, porosity=por, consts=c)
+    area = max(ops.projected_area(solid), 1.0)
+    cd, _ = cd_from(f_post, f, q, u_inlet, area)
+    if return_parts:
+        return cd, q, solid, por
+    return cd

@@ -1,0 +1,140 @@
+"""Hand-written adjoint (dCd/dr, dCd/dq) vs the reference's published FP64
+gradient, vs torch autograd through the CPU oracle (the stand-in for
+jax.grad), vs central finite differences, and the halfway_hard zero."""
+
+import pytest
+import torch
+
+from oracle import drivers
+from oracle.ops import consts_for
+
+pytestmark = pytest.mark.gpu
+
+
+def _sim(nx, ny, nz, tau, collision="mrt", storage="fp64", **kw):
+    from lbm_jax_autodiff_gb300 import Simulation
+    return Simulation(nx, ny, nz, tau, collision=collision, storage=storage, **kw)
+
+
+def test_published_bouzidi_gradient_9333275(cuda):
+    """tests/test_gradients_f64.py:129-217 of the reference: 32x16x16, 10 BGK
+    steps, sigmoid porosity alpha 20, r 0.5, Re 50; published AD 93.33275."""
+    nx, ny, nz = 32, 16, 16
+    tau = 3.0 * (0.05 * 4.0 / 50.0) + 0.5
+    sim = _sim(nx, ny, nz, tau, collision="bgk", storage="fp64")
+    sim.set_sphere(0.5, kind="sigmoid", q_mode="bouzidi", porosity="soft", sharpness=20.0,
+                   disc_floor=1e-20, denom_eps=1e-30)
+    sim.set_state(sim.equilibrium_state())
+    for K in (0, 3):
+        cd, g = sim.cd_and_grad(10, checkpoint_every=K)
+        assert abs(cd - 13.741894179419857) < 1e-9
+        assert abs(g - 93.33275) < 1e-5 * 93.33275, g
+
+
+CASES = [
+    # collision, smag, q_mode, porosity, periodic
+    ("mrt", None, "bouzidi", "soft", True),
+    ("mrt", 0.1, "bouzidi", "hard", True),
+    ("bgk", None, "bouzidi", "hard", False),
+    ("bgk", 0.1, "halfway", "soft", True),
+]
+
+
+@pytest.mark.parametrize("collision,smag,q_mode,porosity,periodic", CASES)
+def test_fp64_vs_autograd(cuda, collision, smag, q_mode, porosity, periodic):
+    nx, ny, nz, n = 24, 12, 12, 8
+    tau = 0.56
+    dt = torch.float64
+    c = consts_for(dt)
+    r = torch.tensor(0.6, dtype=dt, requires_grad=True)
+    cd, q, solid, por = drivers.simulate_cd(r, nx, ny, nz, n, tau, q_mode=q_mode,
+                                            porosity_mode=porosity, collision=collision,
+                                            smagorinsky_cs=smag, periodic_yz=periodic, dtype=dt,
+                                            consts=c, return_parts=True)
+    cd.backward()
+    g_ref = r.grad.item()
+    # dCd/dq with q as a leaf
+    q_leaf = q.detach().clone().requires_grad_(True)
+    cd2 = drivers.simulate_cd(torch.tensor(0.6, dtype=dt), nx, ny, nz, n, tau, q_mode=q_mode,
+                              porosity_mode=porosity, collision=collision, smagorinsky_cs=smag,
+                              periodic_yz=periodic, dtype=dt, consts=c, q_leaf=q_leaf)
+    cd2.backward()
+    gq_ref = q_leaf.grad
+
+    sim = _sim(nx, ny, nz, tau, collision=collision, storage="fp64",
+               use_smagorinsky=smag is not None, smagorinsky_cs=smag or 0.1, periodic_yz=periodic)
+    sim.set_sphere(0.6, kind="sigmoid", q_mode=q_mode, porosity=porosity, sharpness=20.0)
+    sim.set_state(drivers.initial_state(nx, ny, nz, 0.05, dt, c).cuda())
+    cdg, gg, ex = sim.cd_and_grad(n, checkpoint_every=3, dcd_dq=True)
+    assert abs(cdg - cd.item()) <= 1e-10 * abs(cd.item())
+    assert abs(gg - g_ref) <= 1e-8 * max(1.0, abs(g_ref)), (gg, g_ref)
+    gq = ex["dcd_dq"].cpu()
+    links = q >= 0
+    err = (gq[links] - gq_ref[links]).abs().max().item()
+    scale = gq_ref[links].abs().max().item()
+    assert err <= 1e-9 * max(scale, 1.0), (err, scale)
+    assert (gq[~links] == 0).all()
+
+
+def test_halfway_hard_is_exactly_zero(cuda):
+    nx, ny, nz = 32, 16, 16
+    sim = _sim(nx, ny, nz, 0.56, storage="fp32")
+    sim.set_sphere(0.5, kind="sigmoid", q_mode="halfway", porosity="hard")
+    sim.set_state(sim.equilibrium_state())
+    cd, g = sim.cd_and_grad(50, checkpoint_every=10)
+    assert cd > 0.0
+    assert g == 0.0
+
+
+@pytest.mark.parametrize("K", [1, 7, 0])
+def test_checkpoint_interval_invariance(cuda, K):
+    nx, ny, nz = 32, 16, 16
+    sim = _sim(nx, ny, nz, 0.56, storage="fp32")
+    sim.set_sphere(0.5, kind="sigmoid", q_mode="bouzidi", porosity="soft")
+    sim.set_state(sim.equilibrium_state())
+    base = sim.cd_and_grad(30, checkpoint_every=5)
+    got = sim.cd_and_grad(30, checkpoint_every=K)
+    assert got == base      # recomputation is bit-for-bit deterministic
+
+
+def test_fp32_vs_fp64_oracle(cuda):
+    """FP32 storage adjoint within 1e-3 relative of the FP64 oracle gradient."""
+    nx, ny, nz, n = 32, 16, 16, 60
+    tau = 0.56
+    dt = torch.float64
+    r = torch.tensor(0.5, dtype=dt, requires_grad=True)
+    cd = drivers.simulate_cd(r, nx, ny, nz, n, tau, q_mode="bouzidi", porosity_mode="hard",
+                             dtype=dt, consts=consts_for(dt))
+    cd.backward()
+    sim = _sim(nx, ny, nz, tau, storage="fp32")
+    sim.set_sphere(0.5, kind="sigmoid", q_mode="bouzidi", porosity="hard")
+    sim.set_state(sim.equilibrium_state())
+    cdg, gg = sim.cd_and_grad(n, checkpoint_every=20)
+    assert abs(cdg - cd.item()) <= 2e-4 * abs(cd.item())
+    assert abs(gg - r.grad.item()) <= 1e-3 * abs(r.grad.item()), (gg, r.grad.item())
+
+
+def test_central_fd_gpu(cuda):
+    """dCd/dr against central differences of the GPU forward (FP64, dr = 1e-6)."""
+    nx, ny, nz, n = 32, 16, 16, 40
+    tau = 0.56
+
+    def cd_at(rr):
+        s = _sim(nx, ny, nz, tau, storage="fp64")
+        s.set_sphere(rr, kind="sigmoid", q_mode="bouzidi", porosity="soft")
+        s.set_state(s.equilibrium_state())
+        return s.cd_and_grad(n, checkpoint_every=8)
+
+    cd0, g = cd_at(0.55)
+    h = 1e-6
+    fd = (cd_at(0.55 + h)[0] - cd_at(0.55 - h)[0]) / (2 * h)
+    assert abs(fd - g) <= 1e-5 * abs(g), (fd, g)
+
+
+def test_guard_rejected(cuda):
+    from lbm_jax_autodiff_gb300._native import LBMError
+    sim = _sim(16, 8, 8, 0.6, storage="fp32", guard="pre")
+    sim.set_sphere(0.5)
+    sim.set_state(sim.equilibrium_state())
+    with pytest.raises(LBMError, match="UNSUPPORTED"):
+        sim.cd_and_grad(4)

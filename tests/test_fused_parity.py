@@ -65,8 +65,8 @@ def _compare(sim, nx, ny, nz, cfg, n_steps, solid, q, porosity, dtype, ux0, samp
              u_tol=U_TOL, cd_rtol=CD_RTOL, f_tol=None):
     """Run oracle (dtype) and GPU from the same f0; compare u, f and sampled Cd.
 
-    Cd: the GPU value must lie within max(cd_rtol, 4 x the FP32 oracle's own
-    deviation) of the FP64 oracle on the same geometry.  The momentum-exchange
+    Cd: the GPU value must lie within max(cd_rtol, 4 x the FP32 oracle's largest
+    deviation over the run) of the FP64 oracle on the same geometry.  The momentum-exchange
     sum cancels strongly, so an FP32 Cd carries ~1e-4 relative rounding noise
     in transients whichever implementation computes it.
     """
@@ -97,7 +97,10 @@ def _compare(sim, nx, ny, nz, cfg, n_steps, solid, q, porosity, dtype, ux0, samp
             _, ref, _ = _oracle_cds(f0.double(), q.double(), cfg64, n_steps, solid,
                                     None if porosity is None else porosity.double(),
                                     f_ref_guard.double(), c64, sample_every, u_ref)
-            band = [abs(a - b) for a, b in zip(cds, ref)]
+            # noise scale of an FP32 Cd on this run: the FP32 oracle's largest
+            # distance from the FP64 oracle over the sampled steps
+            w = max(abs(a - b) for a, b in zip(cds, ref))
+            band = [w] * len(cds)
         for a, b, w in zip(got, ref, band):
             assert abs(a - b) <= max(cd_rtol * abs(b), CD_NOISE_FACTOR * w) + 1e-12, (got, ref, cds)
     return f_or, f_gpu, cds, samples, resets
