@@ -52,18 +52,22 @@ def up_to_date():
     return all(os.path.getmtime(f) <= t for f in _deps())
 
 
-def build(force=False, verbose=False):
-    """Compile and link; returns the library path."""
-    if not force and up_to_date():
+def build(force=False, verbose=False, extra_flags=(), lib=None):
+    """Compile and link; returns the library path.  ``extra_flags`` (e.g.
+    ``-DLBM_ADJ_MINB=2``) and ``lib`` build a variant next to the default."""
+    out_lib = lib or LIB
+    if not force and not extra_flags and lib is None and up_to_date():
         return LIB
     nvcc = _nvcc()
     os.makedirs(OBJ, exist_ok=True)
     os.makedirs(LIBDIR, exist_ok=True)
     srcs = sources()
 
+    tag = "" if lib is None else "_" + os.path.basename(lib).replace(".so", "")
+
     def compile_one(src):
-        obj = os.path.join(OBJ, os.path.basename(src)[:-3] + ".o")
-        cmd = [nvcc, *NVCC_FLAGS, *ARCH, "-c", src, "-o", obj]
+        obj = os.path.join(OBJ, os.path.basename(src)[:-3] + tag + ".o")
+        cmd = [nvcc, *NVCC_FLAGS, *extra_flags, *ARCH, "-c", src, "-o", obj]
         r = subprocess.run(cmd, capture_output=True, text=True)
         if r.returncode != 0:
             raise RuntimeError("nvcc failed for %s:\n%s\n%s" % (src, " ".join(cmd), r.stderr))
@@ -74,13 +78,13 @@ def build(force=False, verbose=False):
     workers = max(1, min(len(srcs), os.cpu_count() or 4))
     with concurrent.futures.ThreadPoolExecutor(workers) as ex:
         objs = list(ex.map(compile_one, srcs))
-    tmp = LIB + ".tmp"
+    tmp = out_lib + ".tmp"
     cmd = [nvcc, *ARCH, "-shared", "-o", tmp, *objs]
     r = subprocess.run(cmd, capture_output=True, text=True)
     if r.returncode != 0:
         raise RuntimeError("link failed:\n%s\n%s" % (" ".join(cmd), r.stderr))
-    os.replace(tmp, LIB)
-    return LIB
+    os.replace(tmp, out_lib)
+    return out_lib
 
 
 if __name__ == "__main__":

@@ -82,8 +82,55 @@ __device__ __forceinline__ void zou_he_outlet_T(Re l[Q], Re rho_out) {
   for (int j = 0; j < Q; ++j) l[j] = o[j];
 }
 
+// dJ/dq of the wall links owned by a cell at this step, d T(S_k)/dq with
+// S_k = B(c) (c = C(f_k)); accumulates per link and returns the dJ/dr part.
+template <class St>
+__device__ __forceinline__ double link_q_grad(const AdjArgs<typename Storage<St>::Re>& A,
+                                              const typename Storage<St>::Re c[Q],
+                                              typename Storage<St>::Re p, bool soft, bool hard,
+                                              uint32_t ri, int idx, int x, int y, int z) {
+  using Re = typename Storage<St>::Re;
+  using S = Storage<St>;
+  const StepArgs<Re>& a = A.s;
+  const Grid& g = a.g;
+  const size_t N = size_t(g.n);
+  const LinkRec& r = a.rec[ri - 1];
+  const uint32_t lm = r.linkmask;
+  const St* Sk = static_cast<const St*>(A.S_k);
+  double* gq = A.gq + size_t(ri - 1) * Q;
+  double gr = 0.0;
+#pragma unroll
+  for (int i = 1; i < Q; ++i) {
+    const int io = opp(i);
+    if ((lm >> io) & 1u) {
+      const Re qv = Re(r.q[io]);
+      const Re nv = __ldg(A.nu_in + i * N + idx);
+      const Re s_io = soft ? (Re(1) - p) * c[io] + p * c[i] : (hard ? c[i] : c[io]);
+      Re dout;
+      if (qv >= Re(0.5)) {
+        const Re s_i = soft ? (Re(1) - p) * c[i] + p * c[io] : (hard ? c[io] : c[i]);
+        dout = (qv < Re(1)) ? -(s_io - s_i) / (Re(2) * qv * qv) : Re(0);
+      } else {
+        const int nb = ahead_wrap(g, x, y, z, ex(i), ey(i), ez(i));
+        const Re s_nb = S::ld(Sk + io * N + nb, a.K.w[io]);
+        dout = (qv > Re(0)) ? Re(2) * (s_io - s_nb) : Re(0);
+      }
+      const double gqv = double(nv) * double(dout);
+      gq[io] += gqv;
+      gr += gqv * r.dqdr[io];
+    }
+  }
+  return gr;
+}
+
+// resident 256-thread blocks per SM the register allocation is sized for
+#ifndef LBM_ADJ_MINB
+#define LBM_ADJ_MINB 3
+#endif
+
 template <class St, bool MRT>
-__global__ void __launch_bounds__(256, sizeof(St) == 8 ? 1 : 2) k_adjoint(const AdjArgs<typename Storage<St>::Re> A) {
+__global__ void __launch_bounds__(256, sizeof(St) == 8 ? 1 : LBM_ADJ_MINB)
+    k_adjoint(const AdjArgs<typename Storage<St>::Re> A) {
   using Re = typename Storage<St>::Re;
   using S = Storage<St>;
   const StepArgs<Re>& a = A.s;
@@ -94,26 +141,32 @@ __global__ void __launch_bounds__(256, sizeof(St) == 8 ? 1 : 2) k_adjoint(const 
   double gr = 0.0;
 
   if (idx < n) {
-    const int z = idx % g.nz;
-    const int t = idx / g.nz;
-    const int y = t % g.ny;
-    const int x = t / g.ny;
+    int x, y, z;
+    decode(g, idx, x, y, z);
     const uint32_t tag = a.tag ? __ldg(a.tag + idx) : 0u;
     const uint32_t ri = tag & TAG_INDEX;
     const size_t N = size_t(n);
     const Re* nu = A.nu_in;
-    const PullIdx P(g, x, y, z);
 
-    // ---- mu_k = T^T nu_{k+1}: normal-stream part -----------------------
+    // ---- mu_k = T^T nu_{k+1}: normal-stream part (gather from x + e_j) ---
     Re mu[Q];
     mu[0] = __ldg(nu + idx);
+    {
+      const NbrOff O(g, x, y, z);
+      if (!O.face) {
 #pragma unroll
-    for (int j = 1; j < Q; ++j) {
-      // (a) output (y + e_j, j) pulls S_j(y) when that neighbour is in range
-      Re v = P.valid(opp(j)) ? __ldg(nu + j * N + P.raw(opp(j))) : Re(0);
-      // (b) output (y, j) keeps S_j(y) when its own source is out of range
-      if (!P.valid(j)) v += __ldg(nu + j * N + idx);
-      mu[j] = v;
+        for (int j = 1; j < Q; ++j) mu[j] = __ldg(nu + j * N + O.push(j, idx));
+      } else {
+        const PullIdx P(g, x, y, z);
+#pragma unroll
+        for (int j = 1; j < Q; ++j) {
+          // (a) output (y + e_j, j) pulls S_j(y) when that neighbour is in range
+          Re v = P.valid(opp(j)) ? __ldg(nu + j * N + P.raw(opp(j))) : Re(0);
+          // (b) output (y, j) keeps S_j(y) when its own source is out of range
+          if (!P.valid(j)) v += __ldg(nu + j * N + idx);
+          mu[j] = v;
+        }
+      }
     }
 
     // ---- f_k (recompute) --------------------------------------------------
@@ -128,11 +181,11 @@ __global__ void __launch_bounds__(256, sizeof(St) == 8 ? 1 : 2) k_adjoint(const 
 
     // ---- boundary-cell corrections of T^T, force seed --------------------
     if (ri) {
+      const PullIdx P(g, x, y, z);
       const LinkRec& r = a.rec[ri - 1];
       const uint32_t lm = r.linkmask, nbw = r.nb_wall, nbl = r.nb_low;
 #pragma unroll
       for (int j = 1; j < Q; ++j) {
-        // own output j is a wall output: no normal / fallback term
         const bool wall_out = (lm >> opp(j)) & 1u;
         const bool a_ok = P.valid(opp(j)) && !((nbw >> j) & 1u);
         Re v = a_ok ? __ldg(nu + j * N + P.raw(opp(j))) : Re(0);
@@ -166,53 +219,31 @@ __global__ void __launch_bounds__(256, sizeof(St) == 8 ? 1 : 2) k_adjoint(const 
       }
     }
 
-    // ---- collide forward (needed by the porosity / q gradients) ----------
     const bool soft = (fl & (SF_SOLID_SPHERE | SF_SOLID_FIELD)) != 0;
     const bool hard = (fl & SF_SOLID_HARD) && (tag & TAG_SOLID);
-    Re p = Re(0), dpdr = Re(0);
+    Re p = Re(0);
     if (soft) {
+      Re dpdr = Re(0);
       if (fl & SF_SOLID_SPHERE)
         p = sphere_porosity<Re>(a.sph, x, y, z, &dpdr);
       else
         p = a.porosity[idx];
-    }
-    if (soft || ri) {
+      if (ri || (fl & SF_SOLID_SPHERE)) {
+        // dJ/dp = mu . (c[opp] - c) with c = C(f_k)
+        Re c[Q];
+        collide_cell<Re>(f, a.tau, MRT, (fl & SF_SMAG) != 0, a.c18cs2, a.K, c);
+        if (fl & SF_SOLID_SPHERE) {
+          Re gp = Re(0);
+#pragma unroll
+          for (int i = 0; i < Q; ++i) gp += mu[i] * (c[opp(i)] - c[i]);
+          gr += double(gp) * double(dpdr);
+        }
+        if (ri) gr += link_q_grad<St>(A, c, p, true, false, ri, idx, x, y, z);
+      }
+    } else if (ri) {
       Re c[Q];
       collide_cell<Re>(f, a.tau, MRT, (fl & SF_SMAG) != 0, a.c18cs2, a.K, c);
-      if (soft && (fl & SF_SOLID_SPHERE)) {
-        Re gp = Re(0);
-#pragma unroll
-        for (int i = 0; i < Q; ++i) gp += mu[i] * (c[opp(i)] - c[i]);
-        gr += double(gp) * double(dpdr);
-      }
-      if (ri) {
-        // dJ/dq of the links of y at this step: d T(S_k)/dq with S_k = B(c)
-        const LinkRec& r = a.rec[ri - 1];
-        const uint32_t lm = r.linkmask;
-        const St* Sk = static_cast<const St*>(A.S_k);
-        double* gq = A.gq + size_t(ri - 1) * Q;
-#pragma unroll
-        for (int i = 1; i < Q; ++i) {
-          const int io = opp(i);
-          if ((lm >> io) & 1u) {
-            const Re qv = Re(r.q[io]);
-            const Re nv = __ldg(A.nu_in + i * N + idx);
-            const Re s_io = soft ? (Re(1) - p) * c[io] + p * c[i] : (hard ? c[i] : c[io]);
-            Re dout;
-            if (qv >= Re(0.5)) {
-              const Re s_i = soft ? (Re(1) - p) * c[i] + p * c[io] : (hard ? c[io] : c[i]);
-              dout = (qv < Re(1)) ? -(s_io - s_i) / (Re(2) * qv * qv) : Re(0);
-            } else {
-              const int nb = ahead_wrap(g, x, y, z, ex(i), ey(i), ez(i));
-              const Re s_nb = S::ld(Sk + io * N + nb, a.K.w[io]);
-              dout = (qv > Re(0)) ? Re(2) * (s_io - s_nb) : Re(0);
-            }
-            const double gqv = double(nv) * double(dout);
-            gq[io] += gqv;
-            gr += gqv * r.dqdr[io];
-          }
-        }
-      }
+      gr += link_q_grad<St>(A, c, p, false, hard, ri, idx, x, y, z);
     }
 
     // ---- B^T -------------------------------------------------------------
@@ -230,13 +261,14 @@ __global__ void __launch_bounds__(256, sizeof(St) == 8 ? 1 : 2) k_adjoint(const 
       for (int i = 0; i < Q; ++i) mu[i] = m2[i];
     }
 
-    // ---- lambda_k = C^T mu ------------------------------------------------
-    Re lam[Q];
-    collide_vjp<Re>(f, mu, a.tau, MRT, (fl & SF_SMAG) != 0, a.c18cs2, a.K, lam, nullptr);
+    // ---- lambda_k = C^T mu (in place) --------------------------------------
+    CellScalars<Re> cs;
+    cell_scalars<Re>(f, cs);
+    collide_vjp_s<Re>(cs, f, mu, a.tau, MRT, (fl & SF_SMAG) != 0, a.c18cs2, a.K, nullptr);
 
     // ---- nu_k = Z^T lambda_k on the faces ---------------------------------
     if (!A.first) {
-      if (x == g.nx - 1 && !(fl & SF_NO_OUTLET)) zou_he_outlet_T<Re>(lam, a.rho_out);
+      if (x == g.nx - 1 && !(fl & SF_NO_OUTLET)) zou_he_outlet_T<Re>(mu, a.rho_out);
       if (x == 0 && !(fl & SF_NO_INLET)) {
         Re ux = a.u_in[0], uy = a.u_in[1], uz = a.u_in[2];
         if (fl & SF_INLET_FACE) {
@@ -245,27 +277,17 @@ __global__ void __launch_bounds__(256, sizeof(St) == 8 ? 1 : 2) k_adjoint(const 
           uy = a.u_face[fn + fi];
           uz = a.u_face[2 * fn + fi];
         }
-        zou_he_inlet_T<Re>(lam, ux, uy, uz);
+        zou_he_inlet_T<Re>(mu, ux, uy, uz);
       }
     }
 #pragma unroll
-    for (int i = 0; i < Q; ++i) A.nu_out[i * N + idx] = lam[i];
+    for (int i = 0; i < Q; ++i) A.nu_out[i * N + idx] = mu[i];
   }
 
-  // deterministic per-block accumulation of dJ/dr across steps
-  __shared__ double sh[32];
+  // deterministic per-warp accumulation of dJ/dr across steps
 #pragma unroll
   for (int o = 16; o > 0; o >>= 1) gr += __shfl_down_sync(0xffffffffu, gr, o);
-  const int lane = threadIdx.x & 31, wid = threadIdx.x >> 5;
-  if (lane == 0) sh[wid] = gr;
-  __syncthreads();
-  if (wid == 0) {
-    const int nw = (blockDim.x + 31) >> 5;
-    gr = lane < nw ? sh[lane] : 0.0;
-#pragma unroll
-    for (int o = 16; o > 0; o >>= 1) gr += __shfl_down_sync(0xffffffffu, gr, o);
-    if (lane == 0) A.gr_partials[blockIdx.x] += gr;
-  }
+  if ((threadIdx.x & 31) == 0) A.gr_partials[blockIdx.x * 8 + (threadIdx.x >> 5)] += gr;
 }
 
 // nu_N = Z^T lambda_N with lambda_N = dJ/df_N from the momentum exchange:

@@ -391,7 +391,7 @@ int lbm_create(const lbm_params* p, lbm_sim** out) {
   lbm_sim* s = new (std::nothrow) lbm_sim();
   if (!s) return set_error(LBM_ERR_NOMEM, "lbm_create: host allocation failed");
   s->p = *p;
-  s->g = Grid{p->nx, p->ny, p->nz, int(n), p->periodic_yz ? 1 : 0};
+  s->g = make_grid(p->nx, p->ny, p->nz, p->periodic_yz);
   s->n = size_t(n);
   s->st_bytes = p->storage == LBM_F64 ? 8 : (p->storage == LBM_F32 ? 4 : 2);
   s->re_bytes = p->storage == LBM_F64 ? 8 : 4;
@@ -582,7 +582,8 @@ int lbm_cd_and_grad(lbm_sim* s, int n_steps, int checkpoint_every, double* cd_ho
   }
   for (int b = 0; b < 2; ++b)
     if (!s->nu[b]) LBM_TRY(dev_alloc(&s->nu[b], s->n * Q * s->re_bytes));
-  if (!s->gr_partials) LBM_TRY(dev_alloc((void**)&s->gr_partials, size_t(s->nblocks) * sizeof(double)));
+  if (!s->gr_partials)
+    LBM_TRY(dev_alloc((void**)&s->gr_partials, size_t(s->nblocks) * 8 * sizeof(double)));
   if (!s->scal) LBM_TRY(dev_alloc((void**)&s->scal, 8 * sizeof(double)));
   if (s->gq_cap < s->nrec) {
     cudaFree(s->gq);
@@ -614,7 +615,7 @@ int lbm_cd_and_grad(lbm_sim* s, int n_steps, int checkpoint_every, double* cd_ho
   LBM_TRY(cuda_check(launch_dj_dfx(s->scal, dyn_area(s), s->scal + 4, st), "dJ/dFx"));
 
   // ---- backward
-  LBM_TRY(cuda_check(cudaMemsetAsync(s->gr_partials, 0, size_t(s->nblocks) * sizeof(double), st), "memset"));
+  LBM_TRY(cuda_check(cudaMemsetAsync(s->gr_partials, 0, size_t(s->nblocks) * 8 * sizeof(double), st), "memset"));
   LBM_TRY(cuda_check(cudaMemsetAsync(s->gq, 0, size_t(s->gq_cap > 0 ? s->gq_cap : 1) * Q * sizeof(double), st), "memset"));
   int cur = 0;
   LBM_TRY(adjoint_seed(s, s->nu[cur], st));
@@ -636,7 +637,7 @@ int lbm_cd_and_grad(lbm_sim* s, int n_steps, int checkpoint_every, double* cd_ho
       cur = 1 - cur;
     }
   }
-  LBM_TRY(cuda_check(launch_reduce_sum(s->gr_partials, s->nblocks, s->scal + 5, st), "reduce"));
+  LBM_TRY(cuda_check(launch_reduce_sum(s->gr_partials, s->nblocks * 8, s->scal + 5, st), "reduce"));
   if (dcd_dq) {
     cudaError_t e = is_fp64(s)
         ? launch_scatter_gq<double>(s->g, s->tag, s->rec, s->gq, static_cast<double*>(dcd_dq), st)

@@ -496,78 +496,112 @@ __host__ __device__ __forceinline__ Re collide_cell(const Re f[Q], Re tau, bool 
 }
 
 // ---------------------------------------------------------------------------
-// Collision VJP.  Given the pre-collision f and the cotangent lam on the
-// collide output, returns gf = (d collide / d f)^T lam, and g_tau (cotangent of
-// the base tau of this cell; through Smagorinsky when enabled).
+// Collision VJP.  The pre-collision populations enter only through a few
+// per-cell scalars (rho, u and the raw second moments, which also give the
+// MRT stress moments m9, m11, m13, m14, m15), so the VJP works on those and
+// on the cotangent in place, keeping register pressure low.
 //
 // Smagorinsky: d Pi / d s is undefined at Pi = 0 (jax.grad yields NaN there);
 // this implementation uses the subgradient 0.
 // ---------------------------------------------------------------------------
+template <class Re> struct CellScalars {
+  Re rho, ux, uy, uz;
+  Re p[6];   // sum e_a e_b f : xx, yy, zz, xy, xz, yz
+};
+
 template <class Re>
-__host__ __device__ __forceinline__ void collide_vjp(const Re f[Q], const Re lam[Q], Re tau,
-                                                     bool mrt, bool smag, Re c18cs2,
-                                                     const Consts<Re>& K, Re gf[Q],
-                                                     Re* g_tau_out) {
-  const Re rho = density<Re>(f);
+__host__ __device__ __forceinline__ void cell_scalars(const Re f[Q], CellScalars<Re>& c) {
+  c.rho = density<Re>(f);
   Re jx, jy, jz;
   momentum<Re>(f, jx, jy, jz);
+  const Re ir = Re(1) / c.rho;
+  c.ux = jx * ir;
+  c.uy = jy * ir;
+  c.uz = jz * ir;
+  raw_second_moments<Re>(f, c.p);
+}
+
+// g (in: cotangent on the collide output, out: cotangent on f).  ``f`` is
+// only read for BGK when the omega cotangent is needed (Smagorinsky or a
+// requested g_tau): sum_i lam_i (f_i - feq_i).
+template <class Re>
+__host__ __device__ __forceinline__ void collide_vjp_s(const CellScalars<Re>& cs, const Re* f,
+                                                       Re g[Q], Re tau, bool mrt, bool smag,
+                                                       Re c18cs2, const Consts<Re>& K,
+                                                       Re* g_tau_out) {
+  const Re rho = cs.rho, ux = cs.ux, uy = cs.uy, uz = cs.uz;
   const Re ir = Re(1) / rho;
-  const Re ux = jx * ir, uy = jy * ir, uz = jz * ir;
   Re sst[6];
   Re tau_eff = tau, pi = Re(0), R = Re(0), inv_rr = Re(0);
   if (smag) {
-    Re p[6];
-    raw_second_moments<Re>(f, p);
-    neq_stress<Re>(p, K.w, rho, ux, uy, uz, sst);
+    neq_stress<Re>(cs.p, K.w, rho, ux, uy, uz, sst);
     pi = smag_pi<Re>(sst);
     inv_rr = inv_rho_eps<Re>(rho, ir);
     R = sqrt(tau * tau + c18cs2 * pi * inv_rr);
     tau_eff = Re(0.5) * (tau + R);
   }
   const Re omega = Re(1) / tau_eff;
+  const bool want_omega = smag || g_tau_out != nullptr;
   Re g_omega = Re(0);
   Re grho = 0, gx = 0, gy = 0, gz = 0;
   if (mrt) {
-    Re ml[Q], g[Q], m[Q], meq[Q];
-    mrt_moments<Re>(lam, ml);
-    mrt_moments<Re>(f, m);
-    mrt_meq<Re>(rho, ux, uy, uz, meq);
+    Re d[Q];
+    {
+      Re ml[Q];
+      mrt_moments<Re>(g, ml);
 #pragma unroll
-    for (int k = 0; k < Q; ++k) {
-      const Re s = is_stress(k) ? omega : K.rate[k];
-      const Re pk = ml[k] * Re(1.0 / double(mnorm(k)));
-      g[k] = is_conserved(k) ? Re(0) : s * pk;
-      if (is_stress(k)) g_omega -= pk * (m[k] - meq[k]);
+      for (int k = 0; k < Q; ++k) {
+        const Re pk = ml[k] * Re(1.0 / double(mnorm(k)));
+        d[k] = is_conserved(k) ? Re(0) : (is_stress(k) ? omega : K.rate[k]) * pk;
+        if (want_omega && is_stress(k)) {
+          // stress moments of f from the raw second moments
+          Re mk;
+          if (k == 9) mk = Re(2) * cs.p[0] - cs.p[1] - cs.p[2];
+          else if (k == 11) mk = cs.p[1] - cs.p[2];
+          else if (k == 13) mk = cs.p[3];
+          else if (k == 14) mk = cs.p[5];
+          else mk = cs.p[4];
+          Re meqk;
+          if (k == 9) meqk = rho * (Re(2) * ux * ux - uy * uy - uz * uz);
+          else if (k == 11) meqk = rho * (uy * uy - uz * uz);
+          else if (k == 13) meqk = rho * ux * uy;
+          else if (k == 14) meqk = rho * uy * uz;
+          else meqk = rho * ux * uz;
+          g_omega -= pk * (mk - meqk);
+        }
+      }
     }
-    // gf = lam - M^T g
-    mrt_back<Re>(g, lam, gf);
-    // + (d m_eq / d f)^T g, via (rho, u)
-    const Re a9 = g[9] - Re(0.5) * g[10];
-    const Re a11 = g[11] - Re(0.5) * g[12];
+    mrt_back<Re>(d, g, g);   // g <- lam - M^T d (elementwise in place)
+    const Re a9 = d[9] - Re(0.5) * d[10];
+    const Re a11 = d[11] - Re(0.5) * d[12];
     const Re u2 = ux * ux + uy * uy + uz * uz;
     const Re pxx = Re(2) * ux * ux - uy * uy - uz * uz;
     const Re pww = uy * uy - uz * uz;
-    grho = g[1] * (Re(-11) + Re(19) * u2) + g[2] * (Re(3) - Re(5.5) * u2) +
-           Re(-2.0 / 3.0) * (g[4] * ux + g[6] * uy + g[8] * uz) + a9 * pxx + a11 * pww +
-           g[13] * ux * uy + g[14] * uy * uz + g[15] * ux * uz;
-    const Re q12 = Re(38) * g[1] - Re(11) * g[2];
-    gx = rho * (q12 * ux + Re(-2.0 / 3.0) * g[4] + Re(4) * a9 * ux + g[13] * uy + g[15] * uz);
-    gy = rho * (q12 * uy + Re(-2.0 / 3.0) * g[6] - Re(2) * a9 * uy + Re(2) * a11 * uy +
-                g[13] * ux + g[14] * uz);
-    gz = rho * (q12 * uz + Re(-2.0 / 3.0) * g[8] - Re(2) * a9 * uz - Re(2) * a11 * uz +
-                g[14] * uy + g[15] * ux);
+    grho = d[1] * (Re(-11) + Re(19) * u2) + d[2] * (Re(3) - Re(5.5) * u2) +
+           Re(-2.0 / 3.0) * (d[4] * ux + d[6] * uy + d[8] * uz) + a9 * pxx + a11 * pww +
+           d[13] * ux * uy + d[14] * uy * uz + d[15] * ux * uz;
+    const Re q12 = Re(38) * d[1] - Re(11) * d[2];
+    gx = rho * (q12 * ux + Re(-2.0 / 3.0) * d[4] + Re(4) * a9 * ux + d[13] * uy + d[15] * uz);
+    gy = rho * (q12 * uy + Re(-2.0 / 3.0) * d[6] - Re(2) * a9 * uy + Re(2) * a11 * uy +
+                d[13] * ux + d[14] * uz);
+    gz = rho * (q12 * uz + Re(-2.0 / 3.0) * d[8] - Re(2) * a9 * uz - Re(2) * a11 * uz +
+                d[14] * uy + d[15] * ux);
   } else {
-    Re feq[Q], v[Q];
-    equilibrium<Re>(rho, ux, uy, uz, K.w, feq);
+    equilibrium_vjp<Re>(g, rho, ux, uy, uz, K.w, grho, gx, gy, gz);
+    grho *= omega;
+    gx *= omega;
+    gy *= omega;
+    gz *= omega;
+    if (want_omega) {
+      Re feq[Q];
+      equilibrium<Re>(rho, ux, uy, uz, K.w, feq);
 #pragma unroll
-    for (int i = 0; i < Q; ++i) {
-      gf[i] = (Re(1) - omega) * lam[i];
-      v[i] = omega * lam[i];
-      g_omega -= lam[i] * (f[i] - feq[i]);
+      for (int i = 0; i < Q; ++i) g_omega -= g[i] * (f[i] - feq[i]);
     }
-    equilibrium_vjp<Re>(v, rho, ux, uy, uz, K.w, grho, gx, gy, gz);
+#pragma unroll
+    for (int i = 0; i < Q; ++i) g[i] *= (Re(1) - omega);
   }
-  macro_vjp_add<Re>(grho, gx, gy, gz, rho, ux, uy, uz, gf);
+  macro_vjp_add<Re>(grho, gx, gy, gz, rho, ux, uy, uz, g);
 
   // omega = 1 / tau_eff
   const Re g_tau_eff = -g_omega * omega * omega;
@@ -580,7 +614,6 @@ __host__ __device__ __forceinline__ void collide_vjp(const Re f[Q], const Re lam
     const Re g_pi = gX * c18cs2 * inv_rr;
     const Re g_rho_direct = -gX * c18cs2 * pi * inv_rr * inv_rr;
     if (pi > Re(0)) {
-      // d pi / d s (s = xx, yy, zz, xy, xz, yz; off-diagonals counted twice)
       const Re ip = g_pi / pi;
       Re gs[6];
       gs[0] = ip * sst[0];
@@ -600,16 +633,29 @@ __host__ __device__ __forceinline__ void collide_vjp(const Re f[Q], const Re lam
         if (x * y != 0) t += Re(x * y) * gs[3];
         if (x * z != 0) t += Re(x * z) * gs[4];
         if (y * z != 0) t += Re(y * z) * gs[5];
-        gf[i] += t;
+        g[i] += t;
       }
       Re er, exx, eyy, ezz;
       eq_second_vjp<Re>(K.w, rho, ux, uy, uz, gs, er, exx, eyy, ezz);
-      macro_vjp_add<Re>(-er, -exx, -eyy, -ezz, rho, ux, uy, uz, gf);
+      macro_vjp_add<Re>(-er, -exx, -eyy, -ezz, rho, ux, uy, uz, g);
     }
 #pragma unroll
-    for (int i = 0; i < Q; ++i) gf[i] += g_rho_direct;
+    for (int i = 0; i < Q; ++i) g[i] += g_rho_direct;
   }
   if (g_tau_out) *g_tau_out = g_tau;
+}
+
+// Convenience form: gf = (d collide / d f)^T lam.
+template <class Re>
+__host__ __device__ __forceinline__ void collide_vjp(const Re f[Q], const Re lam[Q], Re tau,
+                                                     bool mrt, bool smag, Re c18cs2,
+                                                     const Consts<Re>& K, Re gf[Q],
+                                                     Re* g_tau_out) {
+  CellScalars<Re> cs;
+  cell_scalars<Re>(f, cs);
+#pragma unroll
+  for (int i = 0; i < Q; ++i) gf[i] = lam[i];
+  collide_vjp_s<Re>(cs, f, gf, tau, mrt, smag, c18cs2, K, g_tau_out);
 }
 
 }  // namespace lbm

@@ -27,11 +27,54 @@ struct alignas(16) LinkRec {
   double dqdr[Q];     // d q[j](x) / d r
 };
 
+// Unsigned division by a runtime constant with a multiply-high
+// (Granlund-Montgomery): q = (umulhi(n, mul) + n) >> shift, exact for n < 2^31.
+struct FastDiv {
+  uint32_t d, mul, shift;
+  __host__ __device__ __forceinline__ uint32_t div(uint32_t n) const {
+#ifdef __CUDA_ARCH__
+    return (__umulhi(n, mul) + n) >> shift;
+#else
+    return uint32_t(((uint64_t(n) * mul >> 32) + n) >> shift);
+#endif
+  }
+};
+inline FastDiv make_fastdiv(uint32_t d) {
+  FastDiv f;
+  f.d = d;
+  uint32_t l = 0;
+  while ((1ull << l) < d) ++l;
+  f.shift = l;
+  f.mul = uint32_t(((1ull << 32) * ((1ull << l) - d)) / d + 1);
+  return f;
+}
+
 struct Grid {
   int nx, ny, nz;
   int n;              // nx*ny*nz
   int periodic_yz;
+  FastDiv dz, dy;     // divide by nz, by ny
 };
+
+inline Grid make_grid(int nx, int ny, int nz, int periodic) {
+  Grid g;
+  g.nx = nx;
+  g.ny = ny;
+  g.nz = nz;
+  g.n = nx * ny * nz;
+  g.periodic_yz = periodic ? 1 : 0;
+  g.dz = make_fastdiv(uint32_t(nz));
+  g.dy = make_fastdiv(uint32_t(ny));
+  return g;
+}
+
+__device__ __forceinline__ void decode(const Grid& g, int idx, int& x, int& y, int& z) {
+  const uint32_t t = g.dz.div(uint32_t(idx));
+  z = idx - int(t) * g.nz;
+  const uint32_t xx = g.dy.div(t);
+  y = int(t) - int(xx) * g.ny;
+  x = int(xx);
+}
 
 // flags of StepArgs::flags
 enum : int {
@@ -143,13 +186,13 @@ __device__ __forceinline__ Re sphere_porosity(const SphereP<Re>& s, int x, int y
   return p;
 }
 
-// Guard test of state.py:161-166 / examples/10:164-167 on (rho, j).
+// Guard test of state.py:161-166 / examples/10:164-167 on (rho, j):
+// rho < 0.3, rho > 2, |u| > 0.4 (tested as |j|^2 > 0.16 rho^2, rho being in
+// [0.3, 2] by then), or rho NaN (the first comparison fails for NaN).
 template <class Re>
 __device__ __forceinline__ bool unstable_rj(Re rho, Re jx, Re jy, Re jz) {
-  const Re ir = Re(1) / rho;
-  const Re ux = jx * ir, uy = jy * ir, uz = jz * ir;
-  const Re um = sqrt(ux * ux + uy * uy + uz * uz);
-  return (rho < Re(0.3)) || (rho > Re(2.0)) || (um > Re(0.4)) || (rho != rho);
+  const Re j2 = jx * jx + jy * jy + jz * jz;
+  return !(rho >= Re(0.3) && rho <= Re(2.0)) || (j2 > Re(0.16) * rho * rho);
 }
 
 // Pull offsets of one cell, hoisted out of the 19-direction loop: source
@@ -191,6 +234,36 @@ struct PullIdx {
   }
 };
 
+// Neighbour offsets of a cell away from the domain faces: cell x + d (each
+// component d in {-1,0,1}) is idx + ox[d+1] + oy[d+1] + oz[d+1], with the
+// periodic y/z wrap folded in.  `face` marks cells where some neighbour is
+// out of range (x = 0 / nx-1 always; y/z edges when not periodic); those use
+// PullIdx and its fallback rule.
+struct NbrOff {
+  int ox[3], oy[3], oz[3];
+  bool face;
+  __device__ __forceinline__ NbrOff(const Grid& g, int x, int y, int z) {
+    const int nyz = g.ny * g.nz;
+    ox[0] = -nyz; ox[1] = 0; ox[2] = nyz;
+    oy[0] = -g.nz + (y == 0 ? nyz : 0);
+    oy[1] = 0;
+    oy[2] = g.nz - (y == g.ny - 1 ? nyz : 0);
+    oz[0] = -1 + (z == 0 ? g.nz : 0);
+    oz[1] = 0;
+    oz[2] = 1 - (z == g.nz - 1 ? g.nz : 0);
+    face = (x == 0) || (x == g.nx - 1);
+    if (!g.periodic_yz) face = face || y == 0 || y == g.ny - 1 || z == 0 || z == g.nz - 1;
+  }
+  // source of the pull of direction i: x - e_i
+  __device__ __forceinline__ int pull(int i, int idx) const {
+    return idx + ox[1 - ex(i)] + oy[1 - ey(i)] + oz[1 - ez(i)];
+  }
+  // x + e_j
+  __device__ __forceinline__ int push(int j, int idx) const {
+    return idx + ox[1 + ex(j)] + oy[1 + ey(j)] + oz[1 + ez(j)];
+  }
+};
+
 // Post-stream, post-boundary populations f_k of cell (x,y,z) from the stored
 // post-collision populations S_{k-1}: pull (streaming.py:109-142), Bouzidi on
 // the cell's wall links (streaming.py:148-183), Zou-He inlet/outlet
@@ -204,7 +277,11 @@ __device__ __forceinline__ void pull_post_bc(const StepArgs<typename Storage<St>
   using S = Storage<St>;
   const Grid& g = a.g;
   const size_t N = size_t(g.n);
-  {
+  const NbrOff O(g, x, y, z);
+  if (!O.face) {
+#pragma unroll
+    for (int i = 0; i < Q; ++i) f[i] = S::ld(src + i * N + O.pull(i, idx), a.K.w[i]);
+  } else {
     const PullIdx P(g, x, y, z);
 #pragma unroll
     for (int i = 0; i < Q; ++i) f[i] = S::ld(src + i * N + P.src(i, idx), a.K.w[i]);

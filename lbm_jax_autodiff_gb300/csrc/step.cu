@@ -31,10 +31,8 @@ __global__ void __launch_bounds__(256, sizeof(St) == 8 ? 2 : 4) k_step(const Ste
   unsigned resets = 0;
 
   if (idx < n) {
-    const int z = idx % g.nz;
-    const int t = idx / g.nz;
-    const int y = t % g.ny;
-    const int x = t / g.ny;
+    int x, y, z;
+    decode(g, idx, x, y, z);
     const uint32_t tag = a.tag ? __ldg(a.tag + idx) : 0u;
     const size_t N = size_t(n);
     Re f[Q];

@@ -76,18 +76,19 @@ def channel():
         "profile_ux": ux.tolist(), "l2_vs_parabola": l2, "seconds": time.time() - t0})
 
 
-def sphere():
+def sphere(periodic=False):
     """Config 2: 96x48x48 MRT, Bouzidi hard sphere r=0.5 world (6 cells) at
     world (-2,0,0) = lattice (24,24,24), U 0.05, nu 0.006 (Re 100), free-slip
-    sides, pre-collision guard, 2000 steps, Cd every step of the last 30%."""
+    sides (periodic_yz=False; with periodic=True the examples/10 periodic
+    sides), pre-collision guard, 2000 steps, Cd every step of the last 30%."""
     nx, ny, nz, n = 96, 48, 48, 2000
     U, nu = 0.05, 0.006
     tau = 3 * nu + 0.5
     center = (-2.0, 0.0, 0.0)
     solid, q = geometry.create_sphere(nx, ny, nz, center, 0.5)
     f = drivers.initial_state(nx, ny, nz, U)
-    cfg = drivers.StepConfig(tau=tau, inlet=(U, 0.0, 0.0), collision="mrt", periodic_yz=False,
-                             guard="pre")
+    cfg = drivers.StepConfig(tau=tau, inlet=(U, 0.0, 0.0), collision="mrt",
+                             periodic_yz=periodic, guard="pre")
     area = max(ops.projected_area(solid), 1.0)
     start = n - int(0.3 * n)
     hist = []
@@ -100,13 +101,18 @@ def sphere():
     with torch.no_grad():
         f, _, _ = drivers.run(f, q, cfg, n, solid=solid, f_ref=f, sample_every=1, on_sample=cb)
     u = ops.compute_velocity(f, ops.compute_density(f))
-    np.savez_compressed(os.path.join(HERE, "sphere_96x48x48.npz"),
+    tag = "sphere_96x48x48" + ("_periodic" if periodic else "")
+    np.savez_compressed(os.path.join(HERE, tag + ".npz"),
                         u_sub=u[:, ::2, ::2, ::2].numpy().astype(np.float32))
-    _save_json("sphere_96x48x48.json", {
+    _save_json(tag + ".json", {"periodic_yz": periodic,
         "grid": [nx, ny, nz], "steps": n, "tau": tau, "U": U, "center": center, "radius": 0.5,
         "area": area, "cd_window": [start + 1, n], "cd_mean": float(np.mean(hist)),
         "cd_std": float(np.std(hist)), "cd_last": hist[-1], "cd_hist_every10": hist[::10],
         "links": int((q[1:] >= 0).sum()), "seconds": time.time() - t0})
+
+
+def sphere_periodic():
+    sphere(periodic=True)
 
 
 def modes():
@@ -131,6 +137,6 @@ def modes():
 
 
 if __name__ == "__main__":
-    for name in sys.argv[1:] or ["pins", "channel", "sphere", "modes"]:
+    for name in sys.argv[1:] or ["pins", "channel", "sphere", "sphere_periodic", "modes"]:
         globals()[name]()
         print("done", name, flush=True)
