@@ -201,6 +201,38 @@ def _time_steps(sim, steps, warmup, barrier):
     return e0.elapsed_time(e1) / 1e3
 
 
+def _grad_rate(storage, n_steps, reps, barrier, max_over_ranks, peak, ws):
+    """dCd/dr (bouzidi_hard sphere, MRT + Smagorinsky, no guard) over n_steps:
+    forward with checkpoints, recompute, adjoint; workspace sized to free HBM."""
+    import torch
+    from lbm_jax_autodiff_gb300 import Simulation
+    sim = Simulation(NX, NY, NZ, TAU, collision="mrt", storage=storage, use_smagorinsky=True,
+                     smagorinsky_cs=CS, periodic_yz=True, guard="off",
+                     inlet_velocity=(U, 0.0, 0.0))
+    sim.set_sphere(0.5, center=(0.0, 0.0, 0.0), kind="dist", q_mode="bouzidi", porosity="hard")
+    sim.set_state(sim.equilibrium_state())
+    cd, g = sim.cd_and_grad(n_steps, checkpoint_every=0)      # warm-up, allocates
+    torch.cuda.synchronize()
+    barrier()
+    t0 = time.perf_counter()
+    for _ in range(reps):
+        cd, g = sim.cd_and_grad(n_steps, checkpoint_every=0)
+    t = max_over_ranks((time.perf_counter() - t0) / reps)
+    K, recompute, wbytes = sim.adjoint_plan
+    sim.close()
+    torch.cuda.empty_cache()
+    n_cells = NX * NY * NZ
+    bf = BYTES_PER_UPDATE[storage] / 2          # one population pass, bytes per cell
+    bl = 4.0                                    # adjoint state stays FP32
+    per_cell = (n_steps * 2 * bf + recompute * 2 * bf + n_steps * (bf + 19 * bl * 2))
+    achieved = per_cell * n_cells / t / 1e9
+    return {"evals_per_s": round(ws / t, 4), "s_per_eval": round(t, 4), "steps": n_steps,
+            "cd": cd, "dcd_dr": g, "segment_steps": K, "recomputed_steps": recompute,
+            "workspace_gb": round(wbytes / 1e9, 1),
+            "algorithmic_bytes_per_cell_eval": per_cell,
+            "achieved_gbs": round(achieved, 1), "frac": round(achieved / peak, 4)}
+
+
 def run_ours(args):
     import torch
     ws, rank, local = _dist()
@@ -272,6 +304,16 @@ def run_ours(args):
             "frac": round(BYTES_PER_UPDATE[storage] * n_cells / (t2 / args.steps) / 1e9 / peak, 4),
         }
 
+    # shape gradient: dCd/dr evaluations per second over a 2000-step window
+    grad = {}
+    if not args.no_grad:
+        for storage in ("fp32", "fp16"):
+            grad[storage] = _grad_rate(storage, args.grad_steps, args.grad_reps, barrier,
+                                       max_over_ranks, peak, ws)
+        if grad["fp32"]["evals_per_s"] > 0:
+            grad["fp16_over_fp32"] = round(grad["fp16"]["evals_per_s"] /
+                                           grad["fp32"]["evals_per_s"], 3)
+
     cpu = None
     if rank == 0 and ws == 1 and not args.no_cpu_baseline:
         threads = os.cpu_count() or 1
@@ -306,6 +348,7 @@ def run_ours(args):
             "gpu_launches": args.steps,
             "clocks": clk,
             "storage16": extra,
+            "grad": grad,
             "cd_last_sample": cd_last,
         }
         print(json.dumps(line))
@@ -317,11 +360,14 @@ def run_ours(args):
 def main():
     ap = argparse.ArgumentParser()
     ap.add_argument("--gpus", type=int, default=1)
-    ap.add_argument("--steps", type=int, default=2000)
+    ap.add_argument("--steps", type=int, default=5000)
     ap.add_argument("--warmup", type=int, default=20)
     ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
     ap.add_argument("--steps-ref", type=int, default=3, help="oracle steps in the CPU sample")
     ap.add_argument("--no-cpu-baseline", action="store_true")
+    ap.add_argument("--no-grad", action="store_true", help="skip the dCd/dr measurement")
+    ap.add_argument("--grad-steps", type=int, default=2000)
+    ap.add_argument("--grad-reps", type=int, default=2)
     args = ap.parse_args()
     if args.warmup < 3:
         args.warmup = 3

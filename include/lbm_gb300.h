@@ -127,19 +127,126 @@ int lbm_run(lbm_sim* sim, int n_steps, int sample_every, double* samples, void* 
  * and the sigmoid porosity), as jax.grad of the reference drivers'
  * simulate_cd (examples/11:139-176, examples/08:69-93, tests/
  * test_gradients_f64.py:154-207).  The hand-written adjoint runs backwards
- * with populations checkpointed every `checkpoint_every` steps (<= 0: store
- * every step) and recomputed segment by segment (examples/08:49-66 does the
- * same with jax.checkpoint).  Optional outputs (device, compute dtype, NULL to
+ * with the populations of the last `checkpoint_every` steps kept from the
+ * forward pass and earlier segments of that length recomputed from
+ * checkpoints (examples/08:49-66 does the same with jax.checkpoint);
+ * checkpoint_every <= 0 picks the longest segment that fits in free HBM.
+ * The adjoint workspace is kept in the handle between calls.  Optional outputs (device, compute dtype, NULL to
  * skip): dcd_dq [19][n] = dCd/dq on every link, dcd_df0 [19][n] = dCd/df_0.
  * Requires guard = LBM_GUARD_OFF.  Synchronises `stream`. */
 int lbm_cd_and_grad(lbm_sim* sim, int n_steps, int checkpoint_every, double* cd_host,
                     double* dcd_dr_host, void* dcd_dq, void* dcd_df0, void* stream);
+
+/* Plan of the last lbm_cd_and_grad: segment length, recomputed steps and
+ * the bytes of the population workspace (checkpoints + stash). */
+int lbm_get_adjoint_plan(lbm_sim* sim, int* segment_steps, int* recomputed_steps,
+                         unsigned long long* workspace_bytes);
+/* Free the adjoint population workspace. */
+int lbm_release_workspace(lbm_sim* sim);
 
 /* Host-side queries (synchronise `stream`). */
 int lbm_get_projected_area(lbm_sim* sim, double* area_host);
 int lbm_get_link_count(lbm_sim* sim, int* links_host, int* special_cells_host);
 int lbm_get_guard_resets(lbm_sim* sim, unsigned long long* count_host, void* stream);
 int lbm_get_steps(lbm_sim* sim, long long* steps_host);
+
+/* ---- geometry builders (jax_lbm.geometry), dense outputs -------------------
+ * Synchronise `stream`.  dtype LBM_F32 / LBM_F64 for q, dqdr, porosity. */
+/* solid [n] int32 (may be NULL), q [19][n], dq/dr [19][n] (may be NULL), porosity [n]
+ * (may be NULL: sigmoid field for porosity = SOFT, else the 0/1 mask)
+ * create_sphere (primitives.py:56-174), smooth_sphere_geometry (smooth.py:158-248),
+ * examples/11:56-119 */
+int lbm_sphere_fields(int dtype, int nx, int ny, int nz, const lbm_sphere* sphere,
+                      int32_t* solid, void* q, void* dqdr, void* porosity, void* stream);
+/* create_box: solid inside the world AABB, q = 0.5 on links (primitives.py:177-255) */
+int lbm_box_fields(int dtype, int nx, int ny, int nz, const double* corner_min,
+                   const double* corner_max, int32_t* solid, void* q, void* stream);
+/* compute_q_from_solid (bouzidi.py:32-106) */
+int lbm_q_from_solid(int dtype, const int32_t* solid, double default_q, void* q, int nx, int ny,
+                     int nz, void* stream);
+
+/* ---- per-op drop-ins (jax_lbm.core) --------------------------------------
+ * One launch per reference function; dtype is LBM_F32 or LBM_F64, every array
+ * a device pointer in the reference layout, outputs distinct from inputs.
+ * `flags`: LBM_OP_EXACT_CONSTANTS uses the exact rational weights / MRT rates
+ * instead of the reference's float32-rounded ones (lattice.py:53-60,106-126).
+ * `tau_field` may be NULL (scalar `tau`) or a per-cell [n] field.
+ * The *_vjp entry points are the vector-Jacobian products jax.grad derives for
+ * the same functions; g_* inputs are cotangents of the outputs. */
+#define LBM_OP_EXACT_CONSTANTS 1
+
+/* rho = sum_i f_i                         equilibrium.py:22-48 */
+int lbm_compute_density(int dtype, const void* f, void* rho, int nx, int ny, int nz, void* stream);
+/* u = sum_i f_i e_i / rho                 equilibrium.py:51-87 */
+int lbm_compute_velocity(int dtype, const void* f, const void* rho, void* u, int nx, int ny,
+                         int nz, void* stream);
+/* f_eq(rho, u)                            equilibrium.py:90-151 */
+int lbm_equilibrium(int dtype, const void* rho, const void* u, void* feq, int nx, int ny, int nz,
+                    int flags, void* stream);
+/* f - (f - f_eq) / tau                    collision.py:46-100 */
+int lbm_bgk(int dtype, const void* f, const void* tau_field, double tau, void* out, int nx,
+            int ny, int nz, int flags, void* stream);
+/* MRT collision                           collision.py:103-184 */
+int lbm_mrt(int dtype, const void* f, const void* tau_field, double tau, void* out, int nx,
+            int ny, int nz, int flags, void* stream);
+/* Smagorinsky tau_eff field               collision.py:187-270 */
+int lbm_smagorinsky_tau(int dtype, const void* f, double tau, double cs, void* tau_eff, int nx,
+                        int ny, int nz, int flags, void* stream);
+/* (1 - p) f + p f[opp]                    smooth.py:118-155 */
+int lbm_soft_bounce_back(int dtype, const void* f, const void* porosity, void* out, int nx,
+                         int ny, int nz, void* stream);
+/* pull streaming + Bouzidi, dense q [19][n] streaming.py:40-185 */
+int lbm_stream(int dtype, const void* f, const void* q, int periodic_yz, void* out, int nx, int ny,
+               int nz, void* stream);
+/* Zou-He velocity inlet at x = 0          boundary.py:35-124.  Velocity: u_face [3][ny][nz]
+ * (device, dtype) or, if NULL, velocity[3] (host doubles); rho_target used when has_rho_target. */
+int lbm_zou_he_inlet(int dtype, const void* f, const void* u_face, const double* velocity,
+                     int has_rho_target, double rho_target, void* out, int nx, int ny, int nz,
+                     void* stream);
+/* Zou-He pressure outlet at x = nx-1      boundary.py:127-200 */
+int lbm_zou_he_outlet(int dtype, const void* f, double rho_out, void* out, int nx, int ny, int nz,
+                      void* stream);
+/* F = sum over links of e_i (f*_i + f_opp) into force[3] (device doubles)  forces.py:37-120.
+ * Uses a per-block partial-sum scratch from cudaMallocAsync on `stream`. */
+int lbm_momentum_exchange(int dtype, const void* f_post, const void* f_streamed, const void* q,
+                          double* force, int nx, int ny, int nz, void* stream);
+/* Cd = |Fx| / (0.5 rho U^2 A + 1e-10) into cd[1] (device)  forces.py:237-276 */
+int lbm_drag_coefficient(const double* force, double inlet_velocity, double area, double rho,
+                         double* cd, void* stream);
+/* number of columns along `axis` holding a body cell (solid == 1) into area[1]  forces.py:199-234 */
+int lbm_projected_area(const int32_t* solid, int axis, double* area, int nx, int ny, int nz,
+                       void* stream);
+
+int lbm_compute_density_vjp(int dtype, const void* g_rho, void* g_f, int nx, int ny, int nz,
+                            void* stream);
+int lbm_compute_velocity_vjp(int dtype, const void* f, const void* rho, const void* g_u,
+                             void* g_f, void* g_rho, int nx, int ny, int nz, void* stream);
+int lbm_equilibrium_vjp(int dtype, const void* rho, const void* u, const void* g_feq, void* g_rho,
+                        void* g_u, int nx, int ny, int nz, int flags, void* stream);
+/* g_tau: per-cell cotangent of tau (NULL to skip) */
+int lbm_bgk_vjp(int dtype, const void* f, const void* tau_field, double tau, const void* g_out,
+                void* g_f, void* g_tau, int nx, int ny, int nz, int flags, void* stream);
+int lbm_mrt_vjp(int dtype, const void* f, const void* tau_field, double tau, const void* g_out,
+                void* g_f, void* g_tau, int nx, int ny, int nz, int flags, void* stream);
+/* jax.grad of sqrt at Pi = 0 is NaN; this returns the subgradient 0 there */
+int lbm_smagorinsky_tau_vjp(int dtype, const void* f, double tau, double cs,
+                            const void* g_tau_eff, void* g_f, void* g_tau, int nx, int ny, int nz,
+                            int flags, void* stream);
+int lbm_soft_bounce_back_vjp(int dtype, const void* f, const void* porosity, const void* g_out,
+                             void* g_f, void* g_porosity, int nx, int ny, int nz, void* stream);
+/* g_q (NULL to skip): cotangent of the dense q, non-zero only on links */
+int lbm_stream_vjp(int dtype, const void* f, const void* q, int periodic_yz, const void* g_out,
+                   void* g_f, void* g_q, int nx, int ny, int nz, void* stream);
+/* g_u_face (NULL to skip): [3][ny][nz] cotangent of the inlet velocity */
+int lbm_zou_he_inlet_vjp(int dtype, const void* f, const void* u_face, const double* velocity,
+                         int has_rho_target, double rho_target, const void* g_out, void* g_f,
+                         void* g_u_face, int nx, int ny, int nz, void* stream);
+/* g_rho_out_face (NULL to skip): [ny][nz] per-face-cell cotangent of rho_out */
+int lbm_zou_he_outlet_vjp(int dtype, const void* f, double rho_out, const void* g_out, void* g_f,
+                          void* g_rho_out_face, int nx, int ny, int nz, void* stream);
+/* g_force: device doubles [3] */
+int lbm_momentum_exchange_vjp(int dtype, const void* q, const double* g_force, void* g_f_post,
+                              void* g_f_streamed, int nx, int ny, int nz, void* stream);
 
 #ifdef __cplusplus
 }

@@ -100,6 +100,39 @@ SIGNATURES = {
     "lbm_get_link_count": [_vp, ctypes.POINTER(_i), ctypes.POINTER(_i)],
     "lbm_get_guard_resets": [_vp, ctypes.POINTER(ctypes.c_ulonglong), _vp],
     "lbm_get_steps": [_vp, ctypes.POINTER(_ll)],
+    "lbm_get_adjoint_plan": [_vp, ctypes.POINTER(_i), ctypes.POINTER(_i),
+                             ctypes.POINTER(ctypes.c_ulonglong)],
+    "lbm_release_workspace": [_vp],
+    # geometry builders
+    "lbm_sphere_fields": [_i, _i, _i, _i, ctypes.POINTER(LBMSphereC), _vp, _vp, _vp, _vp, _vp],
+    "lbm_box_fields": [_i, _i, _i, _i, ctypes.POINTER(_d), ctypes.POINTER(_d), _vp, _vp, _vp],
+    "lbm_q_from_solid": [_i, _vp, _d, _vp, _i, _i, _i, _vp],
+    # per-op drop-ins
+    "lbm_compute_density": [_i, _vp, _vp, _i, _i, _i, _vp],
+    "lbm_compute_velocity": [_i, _vp, _vp, _vp, _i, _i, _i, _vp],
+    "lbm_equilibrium": [_i, _vp, _vp, _vp, _i, _i, _i, _i, _vp],
+    "lbm_bgk": [_i, _vp, _vp, _d, _vp, _i, _i, _i, _i, _vp],
+    "lbm_mrt": [_i, _vp, _vp, _d, _vp, _i, _i, _i, _i, _vp],
+    "lbm_smagorinsky_tau": [_i, _vp, _d, _d, _vp, _i, _i, _i, _i, _vp],
+    "lbm_soft_bounce_back": [_i, _vp, _vp, _vp, _i, _i, _i, _vp],
+    "lbm_stream": [_i, _vp, _vp, _i, _vp, _i, _i, _i, _vp],
+    "lbm_zou_he_inlet": [_i, _vp, _vp, ctypes.POINTER(_d), _i, _d, _vp, _i, _i, _i, _vp],
+    "lbm_zou_he_outlet": [_i, _vp, _d, _vp, _i, _i, _i, _vp],
+    "lbm_momentum_exchange": [_i, _vp, _vp, _vp, _vp, _i, _i, _i, _vp],
+    "lbm_drag_coefficient": [_vp, _d, _d, _d, _vp, _vp],
+    "lbm_projected_area": [_vp, _i, _vp, _i, _i, _i, _vp],
+    "lbm_compute_density_vjp": [_i, _vp, _vp, _i, _i, _i, _vp],
+    "lbm_compute_velocity_vjp": [_i, _vp, _vp, _vp, _vp, _vp, _i, _i, _i, _vp],
+    "lbm_equilibrium_vjp": [_i, _vp, _vp, _vp, _vp, _vp, _i, _i, _i, _i, _vp],
+    "lbm_bgk_vjp": [_i, _vp, _vp, _d, _vp, _vp, _vp, _i, _i, _i, _i, _vp],
+    "lbm_mrt_vjp": [_i, _vp, _vp, _d, _vp, _vp, _vp, _i, _i, _i, _i, _vp],
+    "lbm_smagorinsky_tau_vjp": [_i, _vp, _d, _d, _vp, _vp, _vp, _i, _i, _i, _i, _vp],
+    "lbm_soft_bounce_back_vjp": [_i, _vp, _vp, _vp, _vp, _vp, _i, _i, _i, _vp],
+    "lbm_stream_vjp": [_i, _vp, _vp, _i, _vp, _vp, _vp, _i, _i, _i, _vp],
+    "lbm_zou_he_inlet_vjp": [_i, _vp, _vp, ctypes.POINTER(_d), _i, _d, _vp, _vp, _vp, _i, _i,
+                             _i, _vp],
+    "lbm_zou_he_outlet_vjp": [_i, _vp, _d, _vp, _vp, _vp, _i, _i, _i, _vp],
+    "lbm_momentum_exchange_vjp": [_i, _vp, _vp, _vp, _vp, _i, _i, _i, _vp],
 }
 _RESTYPES = {"lbm_status_string": ctypes.c_char_p, "lbm_last_error": ctypes.c_char_p}
 

@@ -108,12 +108,16 @@ __device__ __forceinline__ double link_q_grad(const AdjArgs<typename Storage<St>
       const Re s_io = soft ? (Re(1) - p) * c[io] + p * c[i] : (hard ? c[i] : c[io]);
       Re dout;
       if (qv >= Re(0.5)) {
+        // a = 1 / (2 clip(q, 0.5, 1)); clip passes half the cotangent at a tie
         const Re s_i = soft ? (Re(1) - p) * c[i] + p * c[io] : (hard ? c[io] : c[i]);
-        dout = (qv < Re(1)) ? -(s_io - s_i) / (Re(2) * qv * qv) : Re(0);
+        const Re wc = clip_weight<Re>(qv, Re(0.5), Re(1));
+        const Re qc = fmin(qv, Re(1));
+        dout = wc * (-(s_io - s_i) / (Re(2) * qc * qc));
       } else {
+        // b = 2 clip(q, 0, 0.5)
         const int nb = ahead_wrap(g, x, y, z, ex(i), ey(i), ez(i));
         const Re s_nb = S::ld(Sk + io * N + nb, a.K.w[io]);
-        dout = (qv > Re(0)) ? Re(2) * (s_io - s_nb) : Re(0);
+        dout = clip_weight<Re>(qv, Re(0), Re(0.5)) * Re(2) * (s_io - s_nb);
       }
       const double gqv = double(nv) * double(dout);
       gq[io] += gqv;

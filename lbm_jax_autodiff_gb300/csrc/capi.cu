@@ -37,6 +37,13 @@ cudaError_t launch_classify(const Grid& g, const uint8_t* solid, const Re* q, co
                             uint32_t* tag, LinkRec* rec, int cap, int* counter, int count_only,
                             cudaStream_t st);
 cudaError_t launch_area_cols(const Grid& g, const uint8_t* solid, int* col, cudaStream_t st);
+template <class Re>
+cudaError_t launch_box_fields(const Grid& g, const double lo[3], const double hi[3],
+                              uint8_t* solid, Re* q, cudaStream_t st);
+template <class Re>
+cudaError_t launch_export_fields(const Grid& g, const SphereSpec& s, int with_porosity,
+                                 const uint8_t* solid, int32_t* solid_out, Re* porosity,
+                                 cudaStream_t st);
 
 template <class Re> struct AdjArgs {
   StepArgs<Re> s;
@@ -96,6 +103,9 @@ struct lbm_sim {
   int gq_cap = 0;
   double* gr_partials = nullptr;
   double* scal = nullptr;    // [0..3] F, Cd ; [4] dJ/dFx ; [5] dJ/dr
+  int plan_K = 0;            // last adjoint plan: segment length, recomputed steps, bytes
+  int plan_recompute = 0;
+  size_t plan_bytes = 0;
 };
 
 namespace {
@@ -368,6 +378,36 @@ int set_mask_impl(lbm_sim* s, const int32_t* solid_i32, const void* q_user, doub
 
 }  // namespace
 
+template <class Re>
+static int sphere_fields_impl(int nx, int ny, int nz, const lbm_sphere* sp, int32_t* solid_out,
+                              Re* q, Re* dqdr, Re* porosity, cudaStream_t st) {
+  const Grid g = make_grid(nx, ny, nz, 1);
+  SphereSpec spec;
+  for (int k = 0; k < 3; ++k) spec.c[k] = sp->center[k];
+  spec.r = sp->radius;
+  spec.alpha = sp->sharpness;
+  spec.sigmoid_mask = sp->kind == LBM_SPHERE_SIGMOID_MASK;
+  spec.bouzidi = sp->q_mode == LBM_Q_BOUZIDI;
+  spec.disc_floor = sp->disc_floor;
+  spec.denom_eps = sp->denom_eps;
+  uint8_t* solid = nullptr;
+  Re* dq_tmp = nullptr;
+  LBM_TRY(dev_alloc((void**)&solid, size_t(g.n)));
+  int rc = LBM_OK;
+  do {
+    Re* dq = dqdr;
+    if (!dq && (rc = dev_alloc((void**)&dq_tmp, size_t(g.n) * Q * sizeof(Re)))) break;
+    if (!dq) dq = dq_tmp;
+    if ((rc = cuda_check(launch_sphere_fields<Re>(g, spec, solid, q, dq, st), "sphere fields"))) break;
+    rc = cuda_check(launch_export_fields<Re>(g, spec, sp->porosity == LBM_POROSITY_SOFT, solid,
+                                             solid_out, porosity, st), "export");
+  } while (0);
+  cudaStreamSynchronize(st);
+  cudaFree(solid);
+  cudaFree(dq_tmp);
+  return rc;
+}
+
 extern "C" {
 
 int lbm_api_version(void) { return LBM_GB300_API_VERSION; }
@@ -568,18 +608,7 @@ int lbm_cd_and_grad(lbm_sim* s, int n_steps, int checkpoint_every, double* cd_ho
   LBM_TRY(check_align(dcd_df0, s->re_bytes, "dcd_df0"));
   cudaStream_t st = static_cast<cudaStream_t>(stream);
   const int N = n_steps;
-  int K = checkpoint_every <= 0 ? N : checkpoint_every;
-  if (K > N) K = N;
-  const int nseg = (N + K - 1) / K;
   const size_t state_bytes = s->n * Q * s->st_bytes;
-  const size_t need = size_t(nseg - 1) + size_t(K + 1);
-  if (s->states_cap < need) {
-    cudaFree(s->states);
-    s->states = nullptr;
-    s->states_cap = 0;
-    LBM_TRY(dev_alloc(&s->states, need * state_bytes));
-    s->states_cap = need;
-  }
   for (int b = 0; b < 2; ++b)
     if (!s->nu[b]) LBM_TRY(dev_alloc(&s->nu[b], s->n * Q * s->re_bytes));
   if (!s->gr_partials)
@@ -592,21 +621,57 @@ int lbm_cd_and_grad(lbm_sim* s, int n_steps, int checkpoint_every, double* cd_ho
     LBM_TRY(dev_alloc((void**)&s->gq, size_t(s->nrec > 0 ? s->nrec : 1) * Q * sizeof(double)));
     s->gq_cap = s->nrec;
   }
+  // Segment length K: the last segment's populations come straight from the
+  // forward pass, earlier segments are recomputed from their checkpoints, so
+  // N - K steps are recomputed and ceil(N/K) - 1 + K + 1 states are stored.
+  int K = checkpoint_every;
+  if (K <= 0) {
+    size_t free_b = 0, total_b = 0;
+    LBM_TRY(cuda_check(cudaMemGetInfo(&free_b, &total_b), "cudaMemGetInfo"));
+    free_b += s->states_cap * state_bytes;   // the current workspace is reusable
+    const size_t reserve = (size_t(2) << 30) + total_b / 50;
+    const long long M = free_b > reserve ? (long long)((free_b - reserve) / state_bytes) : 0;
+    K = N;
+    while (K > 1 && (long long)((N + K - 1) / K) + K > M) --K;
+  }
+  if (K > N) K = N;
+  const int nseg = (N + K - 1) / K;
+  const size_t need = size_t(nseg - 1) + size_t(K + 1);
+  if (s->states_cap < need) {
+    cudaFree(s->states);
+    s->states = nullptr;
+    s->states_cap = 0;
+    LBM_TRY(dev_alloc(&s->states, need * state_bytes));
+    s->states_cap = need;
+  }
+  s->plan_K = K;
+  s->plan_recompute = N - K;
+  s->plan_bytes = need * state_bytes;
   char* base = static_cast<char*>(s->states);
-  auto ckpt = [&](int c) -> void* { return base + size_t(c) * state_bytes; };  // S_{(c+1)K-1}
+  auto ckpt = [&](int c) -> void* { return base + size_t(c) * state_bytes; };  // S_{a_{c+1}-1}
   auto stash = [&](int j) -> void* { return base + size_t(nseg - 1 + j) * state_bytes; };
-  const int a_last = (nseg - 1) * K;
+  // segment c covers [seg_a(c), seg_a(c+1)); the last one has exactly K steps
+  auto seg_a = [&](int c) -> int {
+    if (c <= 0) return 0;
+    if (c >= nseg) return N;
+    return N - (nseg - c) * K;
+  };
+  const int a_last = seg_a(nseg - 1);
 
   // ---- forward: checkpoints at segment starts, last segment straight into the stash
   const void* prev = s->fbuf;
+  int next_ck = 1;
   for (int k = 0; k < N; ++k) {
     void* dst;
-    if (k >= a_last)
+    if (k >= a_last) {
       dst = stash(k - a_last + 1);
-    else if ((k + 1) % K == 0)
-      dst = ckpt((k + 1) / K - 1);
-    else
+    } else if (next_ck < nseg && k == seg_a(next_ck) - 1) {
+      dst = ckpt(next_ck - 1);
+      ++next_ck;
+    } else {
       dst = s->S[k & 1];
+      if (dst == prev) dst = s->S[(k + 1) & 1];
+    }
     LBM_TRY(launch(s, prev, dst, k == 0 ? SF_COLLIDE_ONLY : 0, st));
     prev = dst;
   }
@@ -620,7 +685,7 @@ int lbm_cd_and_grad(lbm_sim* s, int n_steps, int checkpoint_every, double* cd_ho
   int cur = 0;
   LBM_TRY(adjoint_seed(s, s->nu[cur], st));
   for (int c = nseg - 1; c >= 0; --c) {
-    const int a0 = c * K, b0 = (a0 + K < N) ? a0 + K : N;
+    const int a0 = seg_a(c), b0 = seg_a(c + 1);
     const void* slot0 = a0 == 0 ? s->fbuf : ckpt(c - 1);
     if (c != nseg - 1) {
       const void* pv = slot0;
@@ -655,6 +720,69 @@ int lbm_cd_and_grad(lbm_sim* s, int n_steps, int checkpoint_every, double* cd_ho
   return LBM_OK;
 }
 
+int lbm_sphere_fields(int dtype, int nx, int ny, int nz, const lbm_sphere* sphere,
+                      int32_t* solid, void* q, void* dqdr, void* porosity, void* stream) {
+  if (!sphere || !q) return set_error(LBM_ERR_ARG, "lbm_sphere_fields: null argument");
+  if (dtype != LBM_F32 && dtype != LBM_F64)
+    return set_error(LBM_ERR_UNSUPPORTED, "lbm_sphere_fields: LBM_F32 or LBM_F64");
+  if (nx < 1 || ny < 1 || nz < 1) return set_error(LBM_ERR_ARG, "lbm_sphere_fields: bad dims");
+  cudaStream_t st = static_cast<cudaStream_t>(stream);
+  if (dtype == LBM_F64)
+    return sphere_fields_impl<double>(nx, ny, nz, sphere, solid, (double*)q, (double*)dqdr,
+                                      (double*)porosity, st);
+  return sphere_fields_impl<float>(nx, ny, nz, sphere, solid, (float*)q, (float*)dqdr,
+                                   (float*)porosity, st);
+}
+
+int lbm_box_fields(int dtype, int nx, int ny, int nz, const double* corner_min,
+                   const double* corner_max, int32_t* solid_out, void* q, void* stream) {
+  if (!corner_min || !corner_max || !q || !solid_out)
+    return set_error(LBM_ERR_ARG, "lbm_box_fields: null argument");
+  if (dtype != LBM_F32 && dtype != LBM_F64)
+    return set_error(LBM_ERR_UNSUPPORTED, "lbm_box_fields: LBM_F32 or LBM_F64");
+  if (nx < 1 || ny < 1 || nz < 1) return set_error(LBM_ERR_ARG, "lbm_box_fields: bad dims");
+  cudaStream_t st = static_cast<cudaStream_t>(stream);
+  const Grid g = make_grid(nx, ny, nz, 1);
+  uint8_t* solid = nullptr;
+  LBM_TRY(dev_alloc((void**)&solid, size_t(g.n)));
+  lbm_sphere none{};
+  SphereSpec spec{};
+  cudaError_t e = dtype == LBM_F64
+      ? launch_box_fields<double>(g, corner_min, corner_max, solid, (double*)q, st)
+      : launch_box_fields<float>(g, corner_min, corner_max, solid, (float*)q, st);
+  int rc = cuda_check(e, "box fields");
+  if (rc == LBM_OK) {
+    e = dtype == LBM_F64
+        ? launch_export_fields<double>(g, spec, 0, solid, solid_out, (double*)nullptr, st)
+        : launch_export_fields<float>(g, spec, 0, solid, solid_out, (float*)nullptr, st);
+    rc = cuda_check(e, "export");
+  }
+  (void)none;
+  cudaStreamSynchronize(st);
+  cudaFree(solid);
+  return rc;
+}
+
+int lbm_q_from_solid(int dtype, const int32_t* solid_i32, double default_q, void* q, int nx,
+                     int ny, int nz, void* stream) {
+  if (!solid_i32 || !q) return set_error(LBM_ERR_ARG, "lbm_q_from_solid: null argument");
+  if (dtype != LBM_F32 && dtype != LBM_F64)
+    return set_error(LBM_ERR_UNSUPPORTED, "lbm_q_from_solid: LBM_F32 or LBM_F64");
+  cudaStream_t st = static_cast<cudaStream_t>(stream);
+  const Grid g = make_grid(nx, ny, nz, 1);
+  uint8_t* solid = nullptr;
+  LBM_TRY(dev_alloc((void**)&solid, size_t(g.n)));
+  int rc = cuda_check(launch_solid_from_i32(g.n, solid_i32, solid, st), "solid");
+  if (rc == LBM_OK) {
+    cudaError_t e = dtype == LBM_F64 ? launch_q_from_solid<double>(g, solid, default_q, (double*)q, st)
+                                     : launch_q_from_solid<float>(g, solid, default_q, (float*)q, st);
+    rc = cuda_check(e, "q from solid");
+  }
+  cudaStreamSynchronize(st);
+  cudaFree(solid);
+  return rc;
+}
+
 int lbm_get_projected_area(lbm_sim* s, double* area_host) {
   if (!s || !area_host) return set_error(LBM_ERR_ARG, "lbm_get_projected_area: null argument");
   if (!s->have_geometry) return set_error(LBM_ERR_STATE, "lbm_get_projected_area: no geometry");
@@ -677,6 +805,24 @@ int lbm_get_guard_resets(lbm_sim* s, unsigned long long* count_host, void* strea
                                      cudaMemcpyDeviceToHost, st),
                      "guard D2H"));
   return cuda_check(cudaStreamSynchronize(st), "sync");
+}
+
+int lbm_get_adjoint_plan(lbm_sim* s, int* segment_steps, int* recomputed_steps,
+                         unsigned long long* workspace_bytes) {
+  if (!s || !segment_steps || !recomputed_steps || !workspace_bytes)
+    return set_error(LBM_ERR_ARG, "lbm_get_adjoint_plan: null argument");
+  *segment_steps = s->plan_K;
+  *recomputed_steps = s->plan_recompute;
+  *workspace_bytes = (unsigned long long)s->plan_bytes;
+  return LBM_OK;
+}
+
+int lbm_release_workspace(lbm_sim* s) {
+  if (!s) return set_error(LBM_ERR_ARG, "lbm_release_workspace: null handle");
+  cudaFree(s->states);
+  s->states = nullptr;
+  s->states_cap = 0;
+  return LBM_OK;
 }
 
 int lbm_get_steps(lbm_sim* s, long long* steps_host) {

@@ -89,8 +89,12 @@ __global__ void k_sphere_q(Grid g, SphereSpec s, const uint8_t* __restrict__ sol
         const Re tt = (-b - sq) / den;
         const bool valid = (disc >= Re(0)) && (tt > Re(0)) && (tt <= Re(1));
         qv = valid ? tt : Re(0.5);
-        if (valid && disc > Re(s.disc_floor) && tt > Re(0.01) && tt < Re(0.99))
-          dq = -(Re(4) * a * r) / (sq * den);
+        if (valid) {
+          // d t / d r through sqrt(max(disc, floor)) and clip(t, 0.01, 0.99),
+          // with jax's half-cotangent rule at ties
+          const Re wmax = disc > Re(s.disc_floor) ? Re(1) : (disc == Re(s.disc_floor) ? Re(0.5) : Re(0));
+          dq = wmax * clip_weight<Re>(tt, Re(0.01), Re(0.99)) * (-(Re(4) * a * r) / (sq * den));
+        }
         qv = fmin(fmax(qv, Re(0.01)), Re(0.99));
       } else {
         qv = Re(0.5);
@@ -175,6 +179,40 @@ __global__ void k_classify(Grid g, const uint8_t* __restrict__ solid, const Re* 
   tag[idx] = sb | uint32_t(ri + 1);
 }
 
+// axis-aligned box, world corners (primitives.py:177-255): solid = inside
+template <class Re>
+__global__ void k_box_solid(Grid g, double x0, double y0, double z0, double x1, double y1,
+                            double z1, uint8_t* __restrict__ solid) {
+  const int idx = blockIdx.x * blockDim.x + threadIdx.x;
+  if (idx >= g.n) return;
+  const int z = idx % g.nz, t = idx / g.nz, y = t % g.ny, x = t / g.ny;
+  Re wx, wy, wz;
+  world<Re>(g, x, y, z, wx, wy, wz);
+  const bool in = wx >= Re(x0) && wx <= Re(x1) && wy >= Re(y0) && wy <= Re(y1) &&
+                  wz >= Re(z0) && wz <= Re(z1);
+  solid[idx] = in ? 1 : 0;
+}
+
+// dense outputs of the builders for the per-op geometry functions
+template <class Re>
+__global__ void k_export_fields(Grid g, SphereSpec s, int with_porosity,
+                                const uint8_t* __restrict__ solid, int32_t* __restrict__ solid_out,
+                                Re* __restrict__ porosity) {
+  const int idx = blockIdx.x * blockDim.x + threadIdx.x;
+  if (idx >= g.n) return;
+  if (solid_out) solid_out[idx] = solid[idx];
+  if (porosity && with_porosity) {
+    const int z = idx % g.nz, t = idx / g.nz, y = t % g.ny, x = t / g.ny;
+    Re wx, wy, wz;
+    world<Re>(g, x, y, z, wx, wy, wz);
+    const Re dx = wx - Re(s.c[0]), dy = wy - Re(s.c[1]), dz = wz - Re(s.c[2]);
+    const Re d = sqrt(dx * dx + dy * dy + dz * dz);
+    porosity[idx] = Re(1) / (Re(1) + exp(-Re(s.alpha) * (Re(s.r) - d)));
+  } else if (porosity) {
+    porosity[idx] = Re(solid[idx] >= 1 ? 1 : 0);
+  }
+}
+
 // column flags for the projected area onto the y-z plane (body cells only)
 __global__ void k_area_cols(Grid g, const uint8_t* __restrict__ solid, int* __restrict__ col) {
   const int idx = blockIdx.x * blockDim.x + threadIdx.x;
@@ -213,6 +251,22 @@ cudaError_t launch_classify(const Grid& g, const uint8_t* solid, const Re* q, co
   return cudaGetLastError();
 }
 
+template <class Re>
+cudaError_t launch_box_fields(const Grid& g, const double lo[3], const double hi[3],
+                              uint8_t* solid, Re* q, cudaStream_t st) {
+  k_box_solid<Re><<<nblk(g.n), 256, 0, st>>>(g, lo[0], lo[1], lo[2], hi[0], hi[1], hi[2], solid);
+  k_q_from_solid<Re><<<nblk(g.n), 256, 0, st>>>(g, solid, Re(0.5), q);
+  return cudaGetLastError();
+}
+
+template <class Re>
+cudaError_t launch_export_fields(const Grid& g, const SphereSpec& s, int with_porosity,
+                                 const uint8_t* solid, int32_t* solid_out, Re* porosity,
+                                 cudaStream_t st) {
+  k_export_fields<Re><<<nblk(g.n), 256, 0, st>>>(g, s, with_porosity, solid, solid_out, porosity);
+  return cudaGetLastError();
+}
+
 cudaError_t launch_area_cols(const Grid& g, const uint8_t* solid, int* col, cudaStream_t st) {
   k_area_cols<<<nblk(g.n), 256, 0, st>>>(g, solid, col);
   return cudaGetLastError();
@@ -226,6 +280,14 @@ template cudaError_t launch_q_from_solid<float>(const Grid&, const uint8_t*, dou
                                                 cudaStream_t);
 template cudaError_t launch_q_from_solid<double>(const Grid&, const uint8_t*, double, double*,
                                                  cudaStream_t);
+template cudaError_t launch_box_fields<float>(const Grid&, const double*, const double*,
+                                              uint8_t*, float*, cudaStream_t);
+template cudaError_t launch_box_fields<double>(const Grid&, const double*, const double*,
+                                               uint8_t*, double*, cudaStream_t);
+template cudaError_t launch_export_fields<float>(const Grid&, const SphereSpec&, int,
+                                                 const uint8_t*, int32_t*, float*, cudaStream_t);
+template cudaError_t launch_export_fields<double>(const Grid&, const SphereSpec&, int,
+                                                  const uint8_t*, int32_t*, double*, cudaStream_t);
 template cudaError_t launch_classify<float>(const Grid&, const uint8_t*, const float*,
                                             const float*, uint32_t*, LinkRec*, int, int*, int,
                                             cudaStream_t);

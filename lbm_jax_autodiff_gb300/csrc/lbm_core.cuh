@@ -121,6 +121,15 @@ template <class Re> struct Consts {
   Re rate[Q];   // fixed MRT rates; stress slots are overwritten by omega
 };
 
+// Derivative weight of clip(x, lo, hi) = min(max(x, lo), hi) under jax's
+// convention: 1 strictly inside, 1/2 at a tie with a bound, 0 outside.
+template <class Re>
+__host__ __device__ __forceinline__ Re clip_weight(Re x, Re lo, Re hi) {
+  if (x > lo && x < hi) return Re(1);
+  if (x == lo || x == hi) return Re(0.5);
+  return Re(0);
+}
+
 // ---------------------------------------------------------------------------
 // Macroscopic moments.
 // ---------------------------------------------------------------------------

@@ -116,7 +116,7 @@ __global__ void __launch_bounds__(256, sizeof(St) == 8 ? 2 : 4) k_step(const Ste
 // the drag coefficient Cd = |Fx| / (0.5 rho U^2 A + 1e-10) (forces.py:274-276).
 // Writes out[0..2] = F, out[3] = Cd.
 __global__ void k_force_finalize(const double* __restrict__ part, int nblocks, double dyn_area,
-                                 double* __restrict__ out) {
+                                 double* __restrict__ out, int with_cd) {
   __shared__ double sh[3][256];
   double a = 0, b = 0, c = 0;
   for (int i = threadIdx.x; i < nblocks; i += blockDim.x) {
@@ -140,7 +140,7 @@ __global__ void k_force_finalize(const double* __restrict__ part, int nblocks, d
     out[0] = sh[0][0];
     out[1] = sh[1][0];
     out[2] = sh[2][0];
-    out[3] = fabs(sh[0][0]) / (dyn_area + 1e-10);
+    if (with_cd) out[3] = fabs(sh[0][0]) / (dyn_area + 1e-10);
   }
 }
 
@@ -158,7 +158,13 @@ cudaError_t launch_step(const StepArgs<typename Storage<St>::Re>& a, bool mrt,
 
 cudaError_t launch_force_finalize(const double* part, int nblocks, double dyn_area, double* out,
                                   cudaStream_t stream) {
-  k_force_finalize<<<1, 256, 0, stream>>>(part, nblocks, dyn_area, out);
+  k_force_finalize<<<1, 256, 0, stream>>>(part, nblocks, dyn_area, out, 1);
+  return cudaGetLastError();
+}
+
+// force only (3 doubles), for the per-op momentum_exchange
+cudaError_t launch_force_sum(const double* part, int nblocks, double* out3, cudaStream_t stream) {
+  k_force_finalize<<<1, 256, 0, stream>>>(part, nblocks, 0.0, out3, 0);
   return cudaGetLastError();
 }
 

@@ -192,7 +192,9 @@ class Simulation:
         "bouzidi") and the sigmoid porosity (porosity "soft"); with
         q_mode "halfway" and porosity "hard" it is exactly 0.0, as in the
         reference's halfway_hard mode.  checkpoint_every=K stores the
-        populations every K steps and recomputes in between (0: keep all).
+        last K steps' populations from the forward pass and recomputes earlier
+        segments of K steps from checkpoints (0: the longest K that fits in
+        free HBM).
         Returns (cd, dcd_dr) or (cd, dcd_dr, extras) when dcd_dq / dcd_df0 are
         requested (dense (19, nx, ny, nz) CUDA tensors).
         """
@@ -209,6 +211,16 @@ class Simulation:
         if extras:
             return cd.value, gr.value, extras
         return cd.value, gr.value
+
+    @property
+    def adjoint_plan(self):
+        """(segment steps, recomputed steps, workspace bytes) of the last cd_and_grad."""
+        a, b, c = ctypes.c_int(), ctypes.c_int(), ctypes.c_ulonglong()
+        nat.call("lbm_get_adjoint_plan", self._h, ctypes.byref(a), ctypes.byref(b), ctypes.byref(c))
+        return a.value, b.value, c.value
+
+    def release_workspace(self):
+        nat.call("lbm_release_workspace", self._h)
 
     # -- queries ------------------------------------------------------------
     @property

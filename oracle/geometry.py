@@ -16,6 +16,7 @@ differentiable exactly as in the reference's traced builders.
 import torch
 
 from .lattice import E, Q
+from .ops import jclip
 
 
 def world_coords(nx, ny, nz, dtype):
@@ -55,11 +56,11 @@ def ray_sphere_q(wx, wy, wz, center, radius, i, nx, ny, nz,
     b = 2.0 * (ox * rdx + oy * rdy + oz * rdz)
     c = ox * ox + oy * oy + oz * oz - radius * radius
     disc = b * b - 4.0 * a * c
-    sq = torch.sqrt(torch.clamp(disc, min=disc_floor))
+    sq = torch.sqrt(jclip(disc, lo=disc_floor))
     t = (-b - sq) / (2.0 * a + a_eps)
     valid = (disc >= 0.0) & (t > 0.0) & (t <= 1.0)
     qv = torch.where(valid, t, torch.full_like(t, 0.5))
-    return torch.clamp(qv, 0.01, 0.99)
+    return jclip(qv, 0.01, 0.99)
 
 
 def create_sphere(nx, ny, nz, center, radius, dtype=torch.float32):

@@ -23,6 +23,33 @@ def consts_for(dtype, ref_consts=True):
     return _DEFAULT[key]
 
 
+class _JaxClip(torch.autograd.Function):
+    """clip(x, lo, hi) with jax's derivative: lax.max/lax.min pass half the
+    cotangent at exact ties (jnp.clip = min(max(x, lo), hi))."""
+
+    @staticmethod
+    def forward(ctx, x, lo, hi):
+        ctx.save_for_backward(x)
+        ctx.lo, ctx.hi = lo, hi
+        return torch.clamp(x, lo, hi)
+
+    @staticmethod
+    def backward(ctx, g):
+        (x,) = ctx.saved_tensors
+        lo, hi = ctx.lo, ctx.hi
+        w = torch.ones_like(x)
+        if lo is not None:
+            w = torch.where(x < lo, torch.zeros_like(w), torch.where(x == lo, 0.5 * w, w))
+        if hi is not None:
+            w = torch.where(x > hi, torch.zeros_like(w), torch.where(x == hi, 0.5 * w, w))
+        return g * w, None, None
+
+
+def jclip(x, lo=None, hi=None):
+    """jnp.clip / jnp.maximum / jnp.minimum with jax's tie rule for gradients."""
+    return _JaxClip.apply(x, lo, hi)
+
+
 def _seq_sum(terms):
     acc = terms[0]
     for t in terms[1:]:
@@ -187,10 +214,10 @@ def stream(f, q, periodic_yz=True):
 
         q_o = q[io]
         has_wall = q_o >= 0.0
-        inv2q = 1.0 / (2.0 * torch.clamp(q_o, 0.5, 1.0))
+        inv2q = 1.0 / (2.0 * jclip(q_o, 0.5, 1.0))
         high = inv2q * f[io] + (1.0 - inv2q) * f[i]
         ahead = torch.roll(f[io], shifts=[-s for s in sh], dims=dims)
-        twoq = 2.0 * torch.clamp(q_o, 0.0, 0.5)
+        twoq = 2.0 * jclip(q_o, 0.0, 0.5)
         low = twoq * f[io] + (1.0 - twoq) * ahead
         bz = torch.where(q_o >= 0.5, high, low)
         out.append(torch.where(has_wall, bz, f_normal))
