@@ -248,6 +248,51 @@ int lbm_zou_he_outlet_vjp(int dtype, const void* f, double rho_out, const void* 
 int lbm_momentum_exchange_vjp(int dtype, const void* q, const double* g_force, void* g_f_post,
                               void* g_f_streamed, int nx, int ny, int nz, void* stream);
 
+/* ---- XLA custom-call targets (jax.ffi, legacy api_version = 0) ------------
+ * Signature: void target(cudaStream_t stream, void** buffers, const char* opaque,
+ * size_t opaque_len); buffers are the operands followed by the results, in the
+ * order of the matching lbm_* entry point above; opaque is one lbm_xla_desc,
+ * either as raw bytes or as the text "lbm1 nx ny nz dtype flags periodic_yz
+ * tau_field u_face has_rho_target tau cs u0 u1 u2 rho" (doubles in C99 hex).
+ * The legacy API has no status: failures are printed to stderr. */
+typedef struct lbm_xla_desc {
+  int32_t nx, ny, nz;
+  int32_t dtype;          /* LBM_F32 / LBM_F64 */
+  int32_t flags;          /* LBM_OP_EXACT_CONSTANTS */
+  int32_t periodic_yz;
+  int32_t tau_field;      /* 1: a per-cell tau operand follows f */
+  int32_t u_face;         /* 1: a [3][ny][nz] inlet-velocity operand follows f */
+  int32_t has_rho_target;
+  int32_t pad;
+  double tau;
+  double cs;
+  double u[3];
+  double rho;             /* rho_target (inlet) or rho_out (outlet) */
+} lbm_xla_desc;
+
+void lbm_xla_compute_density(void* stream, void** buffers, const char* opaque, size_t len);
+void lbm_xla_compute_velocity(void* stream, void** buffers, const char* opaque, size_t len);
+void lbm_xla_equilibrium(void* stream, void** buffers, const char* opaque, size_t len);
+void lbm_xla_bgk(void* stream, void** buffers, const char* opaque, size_t len);
+void lbm_xla_mrt(void* stream, void** buffers, const char* opaque, size_t len);
+void lbm_xla_smagorinsky_tau(void* stream, void** buffers, const char* opaque, size_t len);
+void lbm_xla_soft_bounce_back(void* stream, void** buffers, const char* opaque, size_t len);
+void lbm_xla_stream(void* stream, void** buffers, const char* opaque, size_t len);
+void lbm_xla_zou_he_inlet(void* stream, void** buffers, const char* opaque, size_t len);
+void lbm_xla_zou_he_outlet(void* stream, void** buffers, const char* opaque, size_t len);
+void lbm_xla_momentum_exchange(void* stream, void** buffers, const char* opaque, size_t len);
+void lbm_xla_compute_density_vjp(void* stream, void** buffers, const char* opaque, size_t len);
+void lbm_xla_compute_velocity_vjp(void* stream, void** buffers, const char* opaque, size_t len);
+void lbm_xla_equilibrium_vjp(void* stream, void** buffers, const char* opaque, size_t len);
+void lbm_xla_bgk_vjp(void* stream, void** buffers, const char* opaque, size_t len);
+void lbm_xla_mrt_vjp(void* stream, void** buffers, const char* opaque, size_t len);
+void lbm_xla_smagorinsky_tau_vjp(void* stream, void** buffers, const char* opaque, size_t len);
+void lbm_xla_soft_bounce_back_vjp(void* stream, void** buffers, const char* opaque, size_t len);
+void lbm_xla_stream_vjp(void* stream, void** buffers, const char* opaque, size_t len);
+void lbm_xla_zou_he_inlet_vjp(void* stream, void** buffers, const char* opaque, size_t len);
+void lbm_xla_zou_he_outlet_vjp(void* stream, void** buffers, const char* opaque, size_t len);
+void lbm_xla_momentum_exchange_vjp(void* stream, void** buffers, const char* opaque, size_t len);
+
 #ifdef __cplusplus
 }
 #endif

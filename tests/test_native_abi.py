@@ -41,9 +41,24 @@ def test_every_declared_symbol_is_exported(lib):
 
 
 def test_python_binding_covers_header():
-    from lbm_jax_autodiff_gb300 import _native
-    missing = [n for n in sorted(_declared()) if n not in _native.SIGNATURES]
+    """ctypes prototypes for the C ABI; the XLA custom-call targets are bound
+    by the jax.ffi module."""
+    from lbm_jax_autodiff_gb300 import _native, jax_ffi
+    declared = _declared()
+    missing = [n for n in sorted(declared) if not n.startswith("lbm_xla_")
+               and n not in _native.SIGNATURES]
     assert not missing, missing
+    xla = {n[len("lbm_xla_"):] for n in declared if n.startswith("lbm_xla_")}
+    assert xla == set(jax_ffi.TARGETS)
+
+
+def test_xla_descriptor_text_roundtrip():
+    from lbm_jax_autodiff_gb300 import jax_ffi
+    d = jax_ffi.descriptor(7, 8, 9, 1, flags=1, periodic_yz=0, tau=0.548, cs=0.1,
+                           u=(0.05, -0.01, 0.0), rho=1.02)
+    parts = d.split()
+    assert parts[0] == "lbm1" and parts[1:4] == ["7", "8", "9"]
+    assert float.fromhex(parts[10]) == 0.548 and float.fromhex(parts[15]) == 1.02
 
 
 def test_status_strings_without_gpu(lib):
