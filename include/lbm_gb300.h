@@ -248,6 +248,23 @@ int lbm_zou_he_outlet_vjp(int dtype, const void* f, double rho_out, const void* 
 int lbm_momentum_exchange_vjp(int dtype, const void* q, const double* g_force, void* g_f_post,
                               void* g_f_streamed, int nx, int ny, int nz, void* stream);
 
+/* Same result as lbm_momentum_exchange, but allocates no device memory: for
+ * callers that may not allocate inside a library call -- code running in a
+ * framework that owns all device memory (e.g. an XLA custom call without a
+ * workspace) or under a fixed memory budget.  No counterpart in the
+ * reference.  The partial sums go to a fixed 1.5 MiB array compiled into the
+ * library, which every GPU that loads the library keeps until exit.
+ *  - Grids of at most 16,777,216 cells; larger ones return LBM_ERR_UNSUPPORTED.
+ *  - The first call on a device looks up that array's device address
+ *    (cudaGetSymbolAddress, with that device current); make that first call
+ *    before any stream capture.
+ *  - All calls on a device share the array: calls that overlap on the GPU
+ *    (concurrent streams or threads) race and must be serialised.  Each call
+ *    writes every partial it reads, so nothing needs clearing in between. */
+int lbm_momentum_exchange_noalloc(int dtype, const void* f_post, const void* f_streamed,
+                                  const void* q, double* force, int nx, int ny, int nz,
+                                  void* stream);
+
 /* ---- XLA custom-call targets (jax.ffi, legacy api_version = 0) ------------
  * Signature: void target(cudaStream_t stream, void** buffers, const char* opaque,
  * size_t opaque_len); buffers are the operands followed by the results, in the

@@ -133,6 +133,7 @@ SIGNATURES = {
                              _i, _vp],
     "lbm_zou_he_outlet_vjp": [_i, _vp, _d, _vp, _vp, _vp, _i, _i, _i, _vp],
     "lbm_momentum_exchange_vjp": [_i, _vp, _vp, _vp, _vp, _i, _i, _i, _vp],
+    "lbm_momentum_exchange_noalloc": [_i, _vp, _vp, _vp, _vp, _i, _i, _i, _vp],
 }
 _RESTYPES = {"lbm_status_string": ctypes.c_char_p, "lbm_last_error": ctypes.c_char_p}
 
