@@ -121,6 +121,39 @@ template <class Re> struct Consts {
   Re rate[Q];   // fixed MRT rates; stress slots are overwritten by omega
 };
 
+// Compile-time lattice constants for FP32 arithmetic.  Rounded to float, the
+// exact weights 1/3, 1/18, 1/36 and the reference's float32 weights
+// (lattice.py:53-60) are the same numbers, and so are the MRT rates
+// (lattice.py:106-126); a kernel computing in FP32 can therefore take them
+// as immediates instead of reading them from the parameter bank.
+struct FixedWeightsF {
+  __host__ __device__ constexpr float operator[](int i) const {
+    return i == 0 ? float(1.0 / 3.0) : (i < 7 ? float(1.0 / 18.0) : float(1.0 / 36.0));
+  }
+};
+struct FixedRatesF {
+  __host__ __device__ constexpr float operator[](int k) const {
+    return k == 1 ? float(1.19)
+         : (k == 2 || k == 10 || k == 12) ? float(1.4)
+         : (k == 4 || k == 6 || k == 8) ? float(1.2)
+         : (k >= 16) ? float(1.98) : 0.0f;
+  }
+};
+struct FixedConstsF {
+  FixedWeightsF w;
+  FixedRatesF rate;
+};
+
+// Scalar type of an arithmetic type (a packed two-lane type names its lane
+// type) and whether that scalar is 32-bit.
+template <class Re> struct ScalarOf { using type = Re; };
+template <class Re> struct IsSingle {
+  static constexpr bool value = sizeof(typename ScalarOf<Re>::type) == 4;
+};
+
+__host__ __device__ __forceinline__ float lbm_sqrt(float x) { return sqrtf(x); }
+__host__ __device__ __forceinline__ double lbm_sqrt(double x) { return sqrt(x); }
+
 // Derivative weight of clip(x, lo, hi) = min(max(x, lo), hi) under jax's
 // convention: 1 strictly inside, 1/2 at a tie with a bound, 0 outside.
 template <class Re>
@@ -162,22 +195,22 @@ __host__ __device__ __forceinline__ Re edotu(int i, Re ux, Re uy, Re uz) {
 }
 
 // f_eq_i = w_i rho (1 + 3 eu + 4.5 eu^2 - 1.5 u^2)   (equilibrium.py:144-149)
-template <class Re>
-__host__ __device__ __forceinline__ void equilibrium(Re rho, Re ux, Re uy, Re uz, const Re w[Q],
+template <class Re, class W>
+__host__ __device__ __forceinline__ void equilibrium(Re rho, Re ux, Re uy, Re uz, const W& w,
                                             Re feq[Q]) {
   const Re usq = ux * ux + uy * uy + uz * uz;
   const Re base = Re(1) - Re(1.5) * usq;
 #pragma unroll
   for (int i = 0; i < Q; ++i) {
     const Re eu = edotu<Re>(i, ux, uy, uz);
-    feq[i] = w[i] * rho * (base + eu * (Re(3) + Re(4.5) * eu));
+    feq[i] = Re(w[i]) * rho * (base + eu * (Re(3) + Re(4.5) * eu));
   }
 }
 
 // Cotangent v on f_eq(rho, u) -> (g_rho, g_u) at fixed (rho, u).
-template <class Re>
+template <class Re, class W>
 __host__ __device__ __forceinline__ void equilibrium_vjp(const Re v[Q], Re rho, Re ux, Re uy, Re uz,
-                                                const Re w[Q], Re& grho, Re& gx, Re& gy,
+                                                const W& w, Re& grho, Re& gx, Re& gy,
                                                 Re& gz) {
   const Re usq = ux * ux + uy * uy + uz * uz;
   const Re base = Re(1) - Re(1.5) * usq;
@@ -185,7 +218,7 @@ __host__ __device__ __forceinline__ void equilibrium_vjp(const Re v[Q], Re rho, 
 #pragma unroll
   for (int i = 0; i < Q; ++i) {
     const Re eu = edotu<Re>(i, ux, uy, uz);
-    const Re vw = v[i] * w[i];
+    const Re vw = v[i] * Re(w[i]);
     sp += vw * (base + eu * (Re(3) + Re(4.5) * eu));
     sw += vw;
     const Re t = vw * (Re(1) + Re(3) * eu);
@@ -361,10 +394,11 @@ __host__ __device__ __forceinline__ void raw_second_moments(const Re f[Q], Re p[
 // with W2 = sum_i w_i e_ix^2 = 2 w_face + 8 w_edge and W22 = sum_i w_i e_ix^2 e_iy^2
 // = 4 w_edge (1/3 and 1/9 for the rational weights; the float32-rounded
 // weights of lattice.py:53-60 shift them by ~1e-8, which this form keeps).
-template <class Re>
-__host__ __device__ __forceinline__ void eq_second(const Re w[Q], Re rho, Re ux, Re uy, Re uz,
+template <class Re, class W>
+__host__ __device__ __forceinline__ void eq_second(const W& w, Re rho, Re ux, Re uy, Re uz,
                                                    Re e[6]) {
-  const Re W2 = Re(2) * w[1] + Re(8) * w[7], W22 = Re(4) * w[7];
+  using Sc = typename ScalarOf<Re>::type;
+  const Re W2 = Re(Sc(2) * Sc(w[1]) + Sc(8) * Sc(w[7])), W22 = Re(Sc(4) * Sc(w[7]));
   const Re xx = ux * ux, yy = uy * uy, zz = uz * uz;
   const Re base = W2 * (Re(1) - Re(1.5) * (xx + yy + zz));
   e[0] = rho * (base + Re(4.5) * (W2 * xx + W22 * (yy + zz)));
@@ -377,11 +411,12 @@ __host__ __device__ __forceinline__ void eq_second(const Re w[Q], Re rho, Re ux,
 }
 
 // Cotangent ge on eq_second -> (g_rho, g_u).
-template <class Re>
-__host__ __device__ __forceinline__ void eq_second_vjp(const Re w[Q], Re rho, Re ux, Re uy,
+template <class Re, class W>
+__host__ __device__ __forceinline__ void eq_second_vjp(const W& w, Re rho, Re ux, Re uy,
                                                        Re uz, const Re ge[6], Re& gr, Re& gx,
                                                        Re& gy, Re& gz) {
-  const Re W2 = Re(2) * w[1] + Re(8) * w[7], W22 = Re(4) * w[7];
+  using Sc = typename ScalarOf<Re>::type;
+  const Re W2 = Re(Sc(2) * Sc(w[1]) + Sc(8) * Sc(w[7])), W22 = Re(Sc(4) * Sc(w[7]));
   const Re xx = ux * ux, yy = uy * uy, zz = uz * uz;
   const Re base = W2 * (Re(1) - Re(1.5) * (xx + yy + zz));
   const Re c9 = Re(9) * W22;
@@ -396,8 +431,8 @@ __host__ __device__ __forceinline__ void eq_second_vjp(const Re w[Q], Re rho, Re
 }
 
 // Non-equilibrium stress Pi_ab = sum_i e_ia e_ib f_i - sum_i e_ia e_ib feq_i.
-template <class Re>
-__host__ __device__ __forceinline__ void neq_stress(const Re p[6], const Re w[Q], Re rho, Re ux,
+template <class Re, class W>
+__host__ __device__ __forceinline__ void neq_stress(const Re p[6], const W& w, Re rho, Re ux,
                                                     Re uy, Re uz, Re s[6]) {
   Re e[6];
   eq_second<Re>(w, rho, ux, uy, uz, e);
@@ -407,54 +442,58 @@ __host__ __device__ __forceinline__ void neq_stress(const Re p[6], const Re w[Q]
 
 template <class Re>
 __host__ __device__ __forceinline__ Re smag_pi(const Re s[6]) {
-  return sqrt(s[0] * s[0] + s[1] * s[1] + s[2] * s[2] +
-              Re(2) * (s[3] * s[3] + s[4] * s[4] + s[5] * s[5]));
+  return lbm_sqrt(s[0] * s[0] + s[1] * s[1] + s[2] * s[2] +
+                  Re(2) * (s[3] * s[3] + s[4] * s[4] + s[5] * s[5]));
 }
 
 // 1 / (rho + 1e-10): in float the epsilon is below half an ulp of any
 // physical density, so the reciprocal of rho is reused.
 template <class Re>
 __host__ __device__ __forceinline__ Re inv_rho_eps(Re rho, Re inv_rho) {
-  if (sizeof(Re) == 4) return inv_rho;
+  if (IsSingle<Re>::value) return inv_rho;
   return Re(1) / (rho + Re(1e-10));
 }
 
 template <class Re>
 __host__ __device__ __forceinline__ Re smag_tau(Re tau, Re c18cs2, Re pi, Re inv_rr) {
-  return Re(0.5) * (tau + sqrt(tau * tau + c18cs2 * pi * inv_rr));
+  return Re(0.5) * (tau + lbm_sqrt(tau * tau + c18cs2 * pi * inv_rr));
 }
 
 // ---------------------------------------------------------------------------
 // Collision forward.  ``omega`` = 1 / tau_eff.  BGK: f - omega (f - f_eq).
 // MRT: f - M^-1 S (M f - m_eq), with S = rates and omega in the stress slots.
 // ---------------------------------------------------------------------------
-template <class Re>
+template <class Re, class W>
 __host__ __device__ __forceinline__ void bgk_collide(const Re f[Q], Re rho, Re ux, Re uy, Re uz,
-                                            Re omega, const Re w[Q], Re out[Q]) {
+                                            Re omega, const W& w, Re out[Q]) {
   Re feq[Q];
   equilibrium<Re>(rho, ux, uy, uz, w, feq);
 #pragma unroll
   for (int i = 0; i < Q; ++i) out[i] = f[i] - omega * (f[i] - feq[i]);
 }
 
-template <class Re>
+template <class Re, class RT>
 __host__ __device__ __forceinline__ void mrt_relax_back(const Re f[Q], const Re m[Q], Re rho,
                                                         Re ux, Re uy, Re uz, Re omega,
-                                                        const Re rate[Q], Re out[Q]) {
+                                                        const RT& rate, Re out[Q]) {
+  using Sc = typename ScalarOf<Re>::type;
   Re meq[Q], d[Q];
   mrt_meq<Re>(rho, ux, uy, uz, meq);
-  const Re on = omega;
 #pragma unroll
   for (int k = 0; k < Q; ++k) {
-    const Re s = is_stress(k) ? on : rate[k];
-    d[k] = is_conserved(k) ? Re(0) : (s * Re(1.0 / double(mnorm(k)))) * (m[k] - meq[k]);
+    const Sc inv_norm = Sc(1.0 / double(mnorm(k)));
+    // rows 16-18 have a zero equilibrium moment
+    const Re dm = k >= 16 ? m[k] : m[k] - meq[k];
+    if (is_conserved(k)) d[k] = Re(0);
+    else if (is_stress(k)) d[k] = (omega * Re(inv_norm)) * dm;
+    else d[k] = Re(Sc(rate[k]) * inv_norm) * dm;
   }
   mrt_back<Re>(d, f, out);
 }
 
-template <class Re>
+template <class Re, class RT>
 __host__ __device__ __forceinline__ void mrt_collide(const Re f[Q], Re rho, Re ux, Re uy, Re uz,
-                                            Re omega, const Re rate[Q], Re out[Q]) {
+                                            Re omega, const RT& rate, Re out[Q]) {
   Re m[Q];
   mrt_moments<Re>(f, m);
   mrt_relax_back<Re>(f, m, rho, ux, uy, uz, omega, rate, out);
@@ -462,10 +501,10 @@ __host__ __device__ __forceinline__ void mrt_collide(const Re f[Q], Re rho, Re u
 
 // Full collide of one cell given its density and momentum: optional
 // Smagorinsky tau, then BGK/MRT.  Returns omega actually used.
-template <class Re>
+template <class Re, class KT>
 __host__ __device__ __forceinline__ Re collide_cell_rj(const Re f[Q], Re rho, Re jx, Re jy, Re jz,
                                                        Re tau, bool mrt, bool smag, Re c18cs2,
-                                                       const Consts<Re>& K, Re out[Q]) {
+                                                       const KT& K, Re out[Q]) {
   const Re ir = Re(1) / rho;
   const Re ux = jx * ir, uy = jy * ir, uz = jz * ir;
   Re omega;
@@ -496,9 +535,9 @@ __host__ __device__ __forceinline__ Re collide_cell_rj(const Re f[Q], Re rho, Re
   return omega;
 }
 
-template <class Re>
+template <class Re, class KT>
 __host__ __device__ __forceinline__ Re collide_cell(const Re f[Q], Re tau, bool mrt, bool smag,
-                                                    Re c18cs2, const Consts<Re>& K, Re out[Q]) {
+                                                    Re c18cs2, const KT& K, Re out[Q]) {
   Re jx, jy, jz;
   momentum<Re>(f, jx, jy, jz);
   return collide_cell_rj<Re>(f, density<Re>(f), jx, jy, jz, tau, mrt, smag, c18cs2, K, out);
@@ -533,10 +572,10 @@ __host__ __device__ __forceinline__ void cell_scalars(const Re f[Q], CellScalars
 // g (in: cotangent on the collide output, out: cotangent on f).  ``f`` is
 // only read for BGK when the omega cotangent is needed (Smagorinsky or a
 // requested g_tau): sum_i lam_i (f_i - feq_i).
-template <class Re>
+template <class Re, class KT>
 __host__ __device__ __forceinline__ void collide_vjp_s(const CellScalars<Re>& cs, const Re* f,
                                                        Re g[Q], Re tau, bool mrt, bool smag,
-                                                       Re c18cs2, const Consts<Re>& K,
+                                                       Re c18cs2, const KT& K,
                                                        Re* g_tau_out) {
   const Re rho = cs.rho, ux = cs.ux, uy = cs.uy, uz = cs.uz;
   const Re ir = Re(1) / rho;
@@ -546,7 +585,7 @@ __host__ __device__ __forceinline__ void collide_vjp_s(const CellScalars<Re>& cs
     neq_stress<Re>(cs.p, K.w, rho, ux, uy, uz, sst);
     pi = smag_pi<Re>(sst);
     inv_rr = inv_rho_eps<Re>(rho, ir);
-    R = sqrt(tau * tau + c18cs2 * pi * inv_rr);
+    R = lbm_sqrt(tau * tau + c18cs2 * pi * inv_rr);
     tau_eff = Re(0.5) * (tau + R);
   }
   const Re omega = Re(1) / tau_eff;
@@ -655,10 +694,10 @@ __host__ __device__ __forceinline__ void collide_vjp_s(const CellScalars<Re>& cs
 }
 
 // Convenience form: gf = (d collide / d f)^T lam.
-template <class Re>
+template <class Re, class KT>
 __host__ __device__ __forceinline__ void collide_vjp(const Re f[Q], const Re lam[Q], Re tau,
                                                      bool mrt, bool smag, Re c18cs2,
-                                                     const Consts<Re>& K, Re gf[Q],
+                                                     const KT& K, Re gf[Q],
                                                      Re* g_tau_out) {
   CellScalars<Re> cs;
   cell_scalars<Re>(f, cs);

@@ -15,7 +15,17 @@
 //   store S_k
 // SF_COLLIDE_ONLY (step 0) reads f_0 instead of pulling; SF_STREAM_ONLY stops
 // after f_k and writes it in the reference layout.
+//
+// k_step_pair does the same for two z-adjacent cells per thread (FP32
+// arithmetic, nz even): the 19 populations of both cells live in packed
+// float2 registers and the collision runs on the FP32x2 pipe, the z-aligned
+// directions move as one 4-byte access of two 16-bit values, and the per-cell
+// index and conversion work is shared by the pair.  It serves 16-bit
+// storage; k_step serves FP32 / FP64, odd nz, the COLLIDE_ONLY / STREAM_ONLY
+// launches and the sampled steps that also sum the momentum-exchange force
+// (SF_FORCE).
 #include "sim.cuh"
+#include "vec2.cuh"
 
 namespace lbm {
 
@@ -86,7 +96,11 @@ __global__ void __launch_bounds__(256, sizeof(St) == 8 ? 2 : 4) k_step(const Ste
         ++resets;
       }
       Re c[Q];
-      collide_cell_rj<Re>(f, rho, jx, jy, jz, a.tau, MRT, (fl & SF_SMAG) != 0, a.c18cs2, a.K, c);
+      if constexpr (sizeof(Re) == 4)
+        collide_cell_rj<Re>(f, rho, jx, jy, jz, a.tau, MRT, (fl & SF_SMAG) != 0, a.c18cs2,
+                            FixedConstsF{}, c);
+      else
+        collide_cell_rj<Re>(f, rho, jx, jy, jz, a.tau, MRT, (fl & SF_SMAG) != 0, a.c18cs2, a.K, c);
 
       St* dst = static_cast<St*>(a.dst);
       if ((fl & SF_SOLID_HARD) && (tag & TAG_SOLID)) {
@@ -110,6 +124,143 @@ __global__ void __launch_bounds__(256, sizeof(St) == 8 ? 2 : 4) k_step(const Ste
     const unsigned tot = __reduce_add_sync(0xffffffffu, resets);
     if ((threadIdx.x & 31) == 0 && tot) atomicAdd(a.guard_count, (unsigned long long)tot);
   }
+}
+
+// Per-direction pointers of one pair launch: pull[i] + idx is the interior
+// pull source x - e_i of cell idx in direction i; out[i] + idx its slot in S_k.
+template <class St> struct PairArgs {
+  StepArgs<float> a;
+  const St* pull[Q];
+  St* out[Q];
+};
+
+constexpr int kPairBlock = 128;   // 256 cells per block
+
+// Pre/post guard of state.py:161-169 on both lanes; returns the number of
+// lanes reset (to `reset`, with rho and j recomputed).
+__device__ __forceinline__ unsigned guard_pair(V2 f[Q], V2& rho, V2& jx, V2& jy, V2& jz,
+                                               const float reset[Q]) {
+  const V2 j2 = jx * jx + jy * jy + jz * jz;
+  const V2 lim = V2(0.16f) * rho * rho;
+  const bool b0 = !(rho.x() >= 0.3f && rho.x() <= 2.0f) || j2.x() > lim.x();
+  const bool b1 = !(rho.y() >= 0.3f && rho.y() <= 2.0f) || j2.y() > lim.y();
+  if (b0 || b1) {
+#pragma unroll
+    for (int i = 0; i < Q; ++i) f[i] = V2(b0 ? reset[i] : f[i].x(), b1 ? reset[i] : f[i].y());
+    rho = density<V2>(f);
+    momentum<V2>(f, jx, jy, jz);
+  }
+  return unsigned(b0) + unsigned(b1);
+}
+
+// Everything after the pull for a pair of cells (idx even, z even): guards,
+// Smagorinsky + BGK/MRT collision on the FP32x2 pipe, hard bounce-back or
+// porosity blend, store of S_k through out[i] + idx.
+template <class St, bool MRT>
+__device__ __forceinline__ unsigned finish_pair(const StepArgs<float>& a, St* const* out, int idx,
+                                                int x, int y, int z, uint32_t t0, uint32_t t1,
+                                                V2 f[Q]) {
+  using Pr = Pair<St>;
+  constexpr FixedConstsF K{};
+  const int fl = a.flags;
+  unsigned resets = 0;
+  V2 rho = density<V2>(f);
+  V2 jx, jy, jz;
+  momentum<V2>(f, jx, jy, jz);
+  if (fl & SF_GUARD_POST) resets += guard_pair(f, rho, jx, jy, jz, a.guard_reset);
+  if (fl & SF_GUARD_PRE) resets += guard_pair(f, rho, jx, jy, jz, a.guard_reset);
+
+  V2 c[Q];
+  collide_cell_rj<V2>(f, rho, jx, jy, jz, V2(a.tau), MRT, (fl & SF_SMAG) != 0, V2(a.c18cs2), K, c);
+
+  const bool s0 = (t0 & TAG_SOLID) != 0, s1 = (t1 & TAG_SOLID) != 0;
+  if ((fl & SF_SOLID_HARD) && (s0 || s1)) {
+#pragma unroll
+    for (int i = 0; i < Q; ++i)
+      Pr::st2(out[i] + idx, V2(s0 ? c[opp(i)].x() : c[i].x(), s1 ? c[opp(i)].y() : c[i].y()),
+              K.w[i]);
+  } else if (fl & (SF_SOLID_SPHERE | SF_SOLID_FIELD)) {
+    V2 p;
+    if (fl & SF_SOLID_SPHERE)
+      p = V2(sphere_porosity<float>(a.sph, x, y, z, nullptr),
+             sphere_porosity<float>(a.sph, x, y, z + 1, nullptr));
+    else
+      p = V2(__ldg(reinterpret_cast<const float2*>(a.porosity + idx)));
+    const V2 omp = V2(1.0f) - p;
+#pragma unroll
+    for (int i = 0; i < Q; ++i) Pr::st2(out[i] + idx, omp * c[i] + p * c[opp(i)], K.w[i]);
+  } else {
+#pragma unroll
+    for (int i = 0; i < Q; ++i) Pr::st2(out[i] + idx, c[i], K.w[i]);
+  }
+  return resets;
+}
+
+// Global-memory pull of the lanes marked in `lanes` (bit 0: cell idx, bit 1:
+// idx + 1), with the Bouzidi, Zou-He and fallback rules of pull_post_bc.
+template <class St>
+__device__ __forceinline__ void pull_lanes(const StepArgs<float>& a, int idx, int x, int y, int z,
+                                           uint32_t t0, uint32_t t1, unsigned lanes, V2 f[Q]) {
+  const St* src = static_cast<const St*>(a.src);
+#pragma unroll 1
+  for (int l = 0; l < 2; ++l) {
+    if (!(lanes & (1u << l))) continue;
+    float fl1[Q];
+    pull_post_bc<St>(a, src, idx + l, x, y, z + l, l ? t1 : t0, fl1);
+#pragma unroll
+    for (int i = 0; i < Q; ++i) {
+      if (l) f[i].v.y = fl1[i];
+      else f[i].v.x = fl1[i];
+    }
+  }
+}
+
+__device__ __forceinline__ void add_resets(const StepArgs<float>& a, unsigned resets) {
+  if ((a.flags & (SF_GUARD_PRE | SF_GUARD_POST)) && a.guard_count) {
+    const unsigned tot = __reduce_add_sync(__activemask(), resets);
+    if ((threadIdx.x & 31) == 0 && tot) atomicAdd(a.guard_count, (unsigned long long)tot);
+  }
+}
+
+template <class St, bool MRT>
+__global__ void __launch_bounds__(kPairBlock, 4) k_step_pair(const PairArgs<St> P) {
+  using Pr = Pair<St>;
+  const StepArgs<float>& a = P.a;
+  const Grid& g = a.g;
+  constexpr FixedConstsF K{};
+  const int pidx = blockIdx.x * blockDim.x + threadIdx.x;
+  unsigned resets = 0;
+
+  if (pidx < (g.n >> 1)) {
+    const int idx = pidx << 1;
+    int x, y, z;
+    decode(g, idx, x, y, z);
+    const uint32_t t0 = a.tag ? __ldg(a.tag + idx) : 0u;
+    const uint32_t t1 = a.tag ? __ldg(a.tag + idx + 1) : 0u;
+    bool special = ((t0 | t1) & TAG_INDEX) || x == 0 || x == g.nx - 1;
+    if (!g.periodic_yz) special = special || y == 0 || y == g.ny - 1 || z == 0 || z + 2 == g.nz;
+    V2 f[Q];
+    if (!special) {
+      // interior pair: y wrap shared by both lanes, z wrap per lane
+      const int nyz = g.ny * g.nz;
+      const int iym = idx + (y == 0 ? nyz : 0);          // e_y = +1 pulls y - 1
+      const int iyp = idx - (y == g.ny - 1 ? nyz : 0);   // e_y = -1 pulls y + 1
+      const int zw0 = z == 0 ? g.nz : 0;                 // lane 0, e_z = +1 pulls z - 1
+      const int zw1 = z + 2 == g.nz ? -g.nz : 0;         // lane 1, e_z = -1 pulls z + 2
+#pragma unroll
+      for (int i = 0; i < Q; ++i) {
+        const int b = ey(i) == 1 ? iym : (ey(i) == -1 ? iyp : idx);
+        const St* p = P.pull[i] + b;
+        if (ez(i) == 0) f[i] = Pr::ld2(p, K.w[i]);
+        else if (ez(i) == 1) f[i] = Pr::ld2s(p + zw0, p + 1, K.w[i]);
+        else f[i] = Pr::ld2s(p, p + 1 + zw1, K.w[i]);
+      }
+    } else {
+      pull_lanes<St>(a, idx, x, y, z, t0, t1, 3u, f);
+    }
+    resets = finish_pair<St, MRT>(a, P.out, idx, x, y, z, t0, t1, f);
+  }
+  add_resets(a, resets);
 }
 
 // Deterministic reduction of the per-block force partials (fixed order) and
@@ -144,9 +295,31 @@ __global__ void k_force_finalize(const double* __restrict__ part, int nblocks, d
   }
 }
 
+// FP32 storage runs k_step, the fastest form for it when measured at
+// 256x128x128 (114.6 us vs 118.7 us for k_step_pair); 16-bit storage runs
+// k_step_pair (102.4 us FP16 / 113.5 us BF16 vs 116.7 / 115.7 us), the pair
+// layout halving its conversion and address work per cell.
 template <class St>
 cudaError_t launch_step(const StepArgs<typename Storage<St>::Re>& a, bool mrt,
                         cudaStream_t stream) {
+  if constexpr (sizeof(St) == 2) {
+    if ((a.g.nz % 2) == 0 && !(a.flags & (SF_COLLIDE_ONLY | SF_STREAM_ONLY | SF_FORCE))) {
+      PairArgs<St> P;
+      P.a = a;
+      const Grid& g = a.g;
+      const long long N = g.n, nyz = (long long)g.ny * g.nz;
+      for (int i = 0; i < Q; ++i) {
+        P.pull[i] = static_cast<const St*>(a.src) + i * N - (ex(i) * nyz + ey(i) * g.nz + ez(i));
+        P.out[i] = static_cast<St*>(a.dst) + i * N;
+      }
+      const int nb = (g.n / 2 + kPairBlock - 1) / kPairBlock;
+      if (mrt)
+        k_step_pair<St, true><<<nb, kPairBlock, 0, stream>>>(P);
+      else
+        k_step_pair<St, false><<<nb, kPairBlock, 0, stream>>>(P);
+      return cudaGetLastError();
+    }
+  }
   const int bs = 256;
   const int nb = (a.g.n + bs - 1) / bs;
   if (mrt)
