@@ -21,6 +21,7 @@
 //   lambda_k = C^T B^T mu_k;  nu_k = Z^T lambda_k on the inlet/outlet faces
 #include "capi_util.cuh"
 #include "sim.cuh"
+#include "vec2.cuh"
 
 namespace lbm {
 
@@ -127,6 +128,79 @@ __device__ __forceinline__ double link_q_grad(const AdjArgs<typename Storage<St>
   return gr;
 }
 
+// mu_k(y) = (T_q^T nu_{k+1})(y) for one cell: the gather form of the
+// transposed pull (x + e_j pulled S_j(y)), the fallback terms of out-of-range
+// sources, and on boundary cells the transposed Bouzidi terms and, at the
+// last step, the seed dJ/dS_{N-1} of the momentum exchange.
+template <class Re>
+__device__ __forceinline__ void gather_mu(const AdjArgs<Re>& A, int idx, int x, int y, int z,
+                                          uint32_t tag, Re mu[Q]) {
+  const StepArgs<Re>& a = A.s;
+  const Grid& g = a.g;
+  const size_t N = size_t(g.n);
+  const uint32_t ri = tag & TAG_INDEX;
+  const Re* nu = A.nu_in;
+  // ---- mu_k = T^T nu_{k+1}: normal-stream part (gather from x + e_j) ---
+  mu[0] = __ldg(nu + idx);
+  {
+    const NbrOff O(g, x, y, z);
+    if (!O.face) {
+#pragma unroll
+      for (int j = 1; j < Q; ++j) mu[j] = __ldg(nu + j * N + O.push(j, idx));
+    } else {
+      const PullIdx P(g, x, y, z);
+#pragma unroll
+      for (int j = 1; j < Q; ++j) {
+        // (a) output (y + e_j, j) pulls S_j(y) when that neighbour is in range
+        Re v = P.valid(opp(j)) ? __ldg(nu + j * N + P.raw(opp(j))) : Re(0);
+        // (b) output (y, j) keeps S_j(y) when its own source is out of range
+        if (!P.valid(j)) v += __ldg(nu + j * N + idx);
+        mu[j] = v;
+      }
+    }
+  }
+
+  // ---- boundary-cell corrections of T^T, force seed --------------------
+  if (ri) {
+    const PullIdx P(g, x, y, z);
+    const LinkRec& r = a.rec[ri - 1];
+    const uint32_t lm = r.linkmask, nbw = r.nb_wall, nbl = r.nb_low;
+#pragma unroll
+    for (int j = 1; j < Q; ++j) {
+      const bool wall_out = (lm >> opp(j)) & 1u;
+      const bool a_ok = P.valid(opp(j)) && !((nbw >> j) & 1u);
+      Re v = a_ok ? __ldg(nu + j * N + P.raw(opp(j))) : Re(0);
+      if (!P.valid(j) && !wall_out) v += __ldg(nu + j * N + idx);
+      if ((nbl >> j) & 1u) {
+        const int w = ahead_wrap(g, x, y, z, ex(j), ey(j), ez(j));
+        v += (Re(1) - Re(2) * Re(r.qnb[j])) * __ldg(nu + opp(j) * N + w);
+      }
+      mu[j] = v;
+    }
+#pragma unroll
+    for (int i = 1; i < Q; ++i) {
+      const int io = opp(i);
+      if ((lm >> io) & 1u) {
+        const Re qv = Re(r.q[io]);
+        const Re nv = __ldg(nu + i * N + idx);
+        if (qv >= Re(0.5)) {
+          const Re a2 = Re(1) / (Re(2) * fmin(qv, Re(1)));
+          mu[io] += a2 * nv;
+          mu[i] += (Re(1) - a2) * nv;
+        } else {
+          mu[io] += Re(2) * fmax(qv, Re(0)) * nv;
+        }
+      }
+    }
+    if (A.last) {
+      const Re gfx = Re(*A.dj_dfx);
+#pragma unroll
+      for (int j = 1; j < Q; ++j)
+        if (ex(j) != 0 && ((lm >> j) & 1u)) mu[j] += Re(ex(j)) * gfx;
+    }
+  }
+}
+
 // resident 256-thread blocks per SM the register allocation is sized for
 #ifndef LBM_ADJ_MINB
 #define LBM_ADJ_MINB 3
@@ -152,26 +226,8 @@ __global__ void __launch_bounds__(256, sizeof(St) == 8 ? 1 : LBM_ADJ_MINB)
     const size_t N = size_t(n);
     const Re* nu = A.nu_in;
 
-    // ---- mu_k = T^T nu_{k+1}: normal-stream part (gather from x + e_j) ---
     Re mu[Q];
-    mu[0] = __ldg(nu + idx);
-    {
-      const NbrOff O(g, x, y, z);
-      if (!O.face) {
-#pragma unroll
-        for (int j = 1; j < Q; ++j) mu[j] = __ldg(nu + j * N + O.push(j, idx));
-      } else {
-        const PullIdx P(g, x, y, z);
-#pragma unroll
-        for (int j = 1; j < Q; ++j) {
-          // (a) output (y + e_j, j) pulls S_j(y) when that neighbour is in range
-          Re v = P.valid(opp(j)) ? __ldg(nu + j * N + P.raw(opp(j))) : Re(0);
-          // (b) output (y, j) keeps S_j(y) when its own source is out of range
-          if (!P.valid(j)) v += __ldg(nu + j * N + idx);
-          mu[j] = v;
-        }
-      }
-    }
+    gather_mu<Re>(A, idx, x, y, z, tag, mu);
 
     // ---- f_k (recompute) --------------------------------------------------
     Re f[Q];
@@ -181,46 +237,6 @@ __global__ void __launch_bounds__(256, sizeof(St) == 8 ? 1 : LBM_ADJ_MINB)
       for (int i = 0; i < Q; ++i) f[i] = __ldg(f0 + i * N + idx);
     } else {
       pull_post_bc<St>(a, static_cast<const St*>(a.src), idx, x, y, z, tag, f);
-    }
-
-    // ---- boundary-cell corrections of T^T, force seed --------------------
-    if (ri) {
-      const PullIdx P(g, x, y, z);
-      const LinkRec& r = a.rec[ri - 1];
-      const uint32_t lm = r.linkmask, nbw = r.nb_wall, nbl = r.nb_low;
-#pragma unroll
-      for (int j = 1; j < Q; ++j) {
-        const bool wall_out = (lm >> opp(j)) & 1u;
-        const bool a_ok = P.valid(opp(j)) && !((nbw >> j) & 1u);
-        Re v = a_ok ? __ldg(nu + j * N + P.raw(opp(j))) : Re(0);
-        if (!P.valid(j) && !wall_out) v += __ldg(nu + j * N + idx);
-        if ((nbl >> j) & 1u) {
-          const int w = ahead_wrap(g, x, y, z, ex(j), ey(j), ez(j));
-          v += (Re(1) - Re(2) * Re(r.qnb[j])) * __ldg(nu + opp(j) * N + w);
-        }
-        mu[j] = v;
-      }
-#pragma unroll
-      for (int i = 1; i < Q; ++i) {
-        const int io = opp(i);
-        if ((lm >> io) & 1u) {
-          const Re qv = Re(r.q[io]);
-          const Re nv = __ldg(nu + i * N + idx);
-          if (qv >= Re(0.5)) {
-            const Re a2 = Re(1) / (Re(2) * fmin(qv, Re(1)));
-            mu[io] += a2 * nv;
-            mu[i] += (Re(1) - a2) * nv;
-          } else {
-            mu[io] += Re(2) * fmax(qv, Re(0)) * nv;
-          }
-        }
-      }
-      if (A.last) {
-        const Re gfx = Re(*A.dj_dfx);
-#pragma unroll
-        for (int j = 1; j < Q; ++j)
-          if (ex(j) != 0 && ((lm >> j) & 1u)) mu[j] += Re(ex(j)) * gfx;
-      }
     }
 
     const bool soft = (fl & (SF_SOLID_SPHERE | SF_SOLID_FIELD)) != 0;
@@ -286,6 +302,170 @@ __global__ void __launch_bounds__(256, sizeof(St) == 8 ? 1 : LBM_ADJ_MINB)
     }
 #pragma unroll
     for (int i = 0; i < Q; ++i) A.nu_out[i * N + idx] = mu[i];
+  }
+
+  // deterministic per-warp accumulation of dJ/dr across steps
+#pragma unroll
+  for (int o = 16; o > 0; o >>= 1) gr += __shfl_down_sync(0xffffffffu, gr, o);
+  if ((threadIdx.x & 31) == 0) A.gr_partials[blockIdx.x * 8 + (threadIdx.x >> 5)] += gr;
+}
+
+// ---------------------------------------------------------------------------
+// k_adjoint_pair: the same adjoint step for two z-adjacent cells per thread
+// (FP32 arithmetic, nz even, no porosity blend): the interior gather of
+// nu_{k+1}, the recomputed f_k and the collision transpose run on packed
+// float2 values (FP32x2 pipe).  Pairs with a boundary record, on an x face or
+// on a non-periodic y/z edge take the per-cell path of k_adjoint lane by lane.
+// ---------------------------------------------------------------------------
+template <class St> struct AdjPairArgs {
+  AdjArgs<float> A;
+  const St* pull[Q];      // S_{k-1} + i N - (e_x nyz + e_y nz + e_z): pull source of cell 0
+  const float* push[Q];   // nu_{k+1} + j N + (e_x nyz + e_y nz + e_z): cell 0 + e_j
+  float* out[Q];          // nu_k + i N
+};
+
+constexpr int kAdjPairBlock = 128;   // 256 cells per block, as k_adjoint
+
+#ifndef LBM_ADJ_PAIR_MINB
+#define LBM_ADJ_PAIR_MINB 3
+#endif
+
+// One cell of a boundary pair: mu, f_k and the dJ/dq terms of its wall links
+// (hard or no solid blend), as k_adjoint computes them.
+template <class St, bool MRT>
+__device__ __forceinline__ double adj_cell_inputs(const AdjArgs<float>& A, int idx, int x, int y,
+                                                  int z, uint32_t tag, float mu[Q], float f[Q]) {
+  const StepArgs<float>& a = A.s;
+  const int fl = a.flags;
+  gather_mu<float>(A, idx, x, y, z, tag, mu);
+  if (A.first) {
+    const float* f0 = static_cast<const float*>(a.src);
+    const size_t N = size_t(a.g.n);
+#pragma unroll
+    for (int i = 0; i < Q; ++i) f[i] = __ldg(f0 + i * N + idx);
+  } else {
+    pull_post_bc<St>(a, static_cast<const St*>(a.src), idx, x, y, z, tag, f);
+  }
+  const uint32_t ri = tag & TAG_INDEX;
+  if (!ri) return 0.0;
+  float c[Q];
+  collide_cell<float>(f, a.tau, MRT, (fl & SF_SMAG) != 0, a.c18cs2, FixedConstsF{}, c);
+  const bool hard = (fl & SF_SOLID_HARD) && (tag & TAG_SOLID);
+  return link_q_grad<St>(A, c, 0.0f, false, hard, ri, idx, x, y, z);
+}
+
+template <class St, bool MRT>
+__global__ void __launch_bounds__(kAdjPairBlock, LBM_ADJ_PAIR_MINB)
+    k_adjoint_pair(const AdjPairArgs<St> P) {
+  using Pr = Pair<St>;
+  const AdjArgs<float>& A = P.A;
+  const StepArgs<float>& a = A.s;
+  const Grid& g = a.g;
+  constexpr FixedConstsF K{};
+  const int pidx = blockIdx.x * blockDim.x + threadIdx.x;
+  const int fl = a.flags;
+  double gr = 0.0;
+
+  if (pidx < (g.n >> 1)) {
+    const int idx = pidx << 1;
+    int x, y, z;
+    decode(g, idx, x, y, z);
+    const uint32_t t0 = a.tag ? __ldg(a.tag + idx) : 0u;
+    const uint32_t t1 = a.tag ? __ldg(a.tag + idx + 1) : 0u;
+    bool special = ((t0 | t1) & TAG_INDEX) || x == 0 || x == g.nx - 1;
+    if (!g.periodic_yz) special = special || y == 0 || y == g.ny - 1 || z == 0 || z + 2 == g.nz;
+    V2 mu[Q], f[Q];
+    if (!special) {
+      const int nyz = g.ny * g.nz;
+      // mu_k(y) = nu_{k+1}(y + e_j): y wrap shared, z wrap per lane
+      {
+        const int iyp = idx - (y == g.ny - 1 ? nyz : 0);   // e_y = +1 reads y + 1
+        const int iym = idx + (y == 0 ? nyz : 0);          // e_y = -1 reads y - 1
+        const int zw1 = z + 2 == g.nz ? -g.nz : 0;         // lane 1, e_z = +1 reads z + 2
+        const int zw0 = z == 0 ? g.nz : 0;                 // lane 0, e_z = -1 reads z - 1
+#pragma unroll
+        for (int j = 0; j < Q; ++j) {
+          const int b = ey(j) == 1 ? iyp : (ey(j) == -1 ? iym : idx);
+          const float* p = P.push[j] + b;
+          if (ez(j) == 0) mu[j] = V2(__ldg(reinterpret_cast<const float2*>(p)));
+          else if (ez(j) == 1) mu[j] = V2(__ldg(p), __ldg(p + 1 + zw1));
+          else mu[j] = V2(__ldg(p + zw0), __ldg(p + 1));
+        }
+      }
+      // f_k
+      if (A.first) {
+        const float* f0 = static_cast<const float*>(a.src);
+        const size_t N = size_t(g.n);
+#pragma unroll
+        for (int i = 0; i < Q; ++i)
+          f[i] = V2(__ldg(reinterpret_cast<const float2*>(f0 + i * N + idx)));
+      } else {
+        const int iym = idx + (y == 0 ? nyz : 0);          // e_y = +1 pulls y - 1
+        const int iyp = idx - (y == g.ny - 1 ? nyz : 0);   // e_y = -1 pulls y + 1
+        const int zw0 = z == 0 ? g.nz : 0;                 // lane 0, e_z = +1 pulls z - 1
+        const int zw1 = z + 2 == g.nz ? -g.nz : 0;         // lane 1, e_z = -1 pulls z + 2
+#pragma unroll
+        for (int i = 0; i < Q; ++i) {
+          const int b = ey(i) == 1 ? iym : (ey(i) == -1 ? iyp : idx);
+          const St* p = P.pull[i] + b;
+          if (ez(i) == 0) f[i] = Pr::ld2(p, K.w[i]);
+          else if (ez(i) == 1) f[i] = Pr::ld2s(p + zw0, p + 1, K.w[i]);
+          else f[i] = Pr::ld2s(p, p + 1 + zw1, K.w[i]);
+        }
+      }
+    } else {
+#pragma unroll 1
+      for (int l = 0; l < 2; ++l) {
+        float m1[Q], f1[Q];
+        gr += adj_cell_inputs<St, MRT>(A, idx + l, x, y, z + l, l ? t1 : t0, m1, f1);
+#pragma unroll
+        for (int i = 0; i < Q; ++i) {
+          if (l) {
+            mu[i].v.y = m1[i];
+            f[i].v.y = f1[i];
+          } else {
+            mu[i].v.x = m1[i];
+            f[i].v.x = f1[i];
+          }
+        }
+      }
+    }
+
+    // B^T of the hard bounce-back: S_i = c_opp(i) on solid cells
+    if (fl & SF_SOLID_HARD) {
+      const bool s0 = (t0 & TAG_SOLID) != 0, s1 = (t1 & TAG_SOLID) != 0;
+      if (s0 || s1) {
+        V2 m2[Q];
+#pragma unroll
+        for (int i = 0; i < Q; ++i)
+          m2[i] = V2(s0 ? mu[opp(i)].x() : mu[i].x(), s1 ? mu[opp(i)].y() : mu[i].y());
+#pragma unroll
+        for (int i = 0; i < Q; ++i) mu[i] = m2[i];
+      }
+    }
+
+    // lambda_k = C^T mu
+    CellScalars<V2> cs;
+    cell_scalars<V2>(f, cs);
+    collide_vjp_s<V2>(cs, f, mu, V2(a.tau), MRT, (fl & SF_SMAG) != 0, V2(a.c18cs2), K,
+                      static_cast<V2*>(nullptr));
+
+    // nu_k = Z^T lambda_k on the faces (both cells of a pair share x)
+    if (!A.first) {
+      if (x == g.nx - 1 && !(fl & SF_NO_OUTLET)) zou_he_outlet_T<V2>(mu, V2(a.rho_out));
+      if (x == 0 && !(fl & SF_NO_INLET)) {
+        V2 ux(a.u_in[0]), uy(a.u_in[1]), uz(a.u_in[2]);
+        if (fl & SF_INLET_FACE) {
+          const int fi = y * g.nz + z, fn = g.ny * g.nz;
+          ux = V2(a.u_face[fi], a.u_face[fi + 1]);
+          uy = V2(a.u_face[fn + fi], a.u_face[fn + fi + 1]);
+          uz = V2(a.u_face[2 * fn + fi], a.u_face[2 * fn + fi + 1]);
+        }
+        zou_he_inlet_T<V2>(mu, ux, uy, uz);
+      }
+    }
+#pragma unroll
+    for (int i = 0; i < Q; ++i) *reinterpret_cast<float2*>(P.out[i] + idx) = mu[i].v;
   }
 
   // deterministic per-warp accumulation of dJ/dr across steps
@@ -373,6 +553,26 @@ static inline int nblk(int n) { return (n + 255) / 256; }
 template <class St>
 cudaError_t launch_adjoint(const AdjArgs<typename Storage<St>::Re>& A, bool mrt,
                            cudaStream_t st) {
+  if constexpr (sizeof(typename Storage<St>::Re) == 4) {
+    const Grid& g = A.s.g;
+    if ((g.nz % 2) == 0 && !(A.s.flags & (SF_SOLID_SPHERE | SF_SOLID_FIELD))) {
+      AdjPairArgs<St> P;
+      P.A = A;
+      const long long N = g.n, nyz = (long long)g.ny * g.nz;
+      for (int i = 0; i < Q; ++i) {
+        const long long off = ex(i) * nyz + ey(i) * g.nz + ez(i);
+        P.pull[i] = static_cast<const St*>(A.s.src) + i * N - off;
+        P.push[i] = A.nu_in + i * N + off;
+        P.out[i] = A.nu_out + i * N;
+      }
+      const int nb = (g.n / 2 + kAdjPairBlock - 1) / kAdjPairBlock;
+      if (mrt)
+        k_adjoint_pair<St, true><<<nb, kAdjPairBlock, 0, st>>>(P);
+      else
+        k_adjoint_pair<St, false><<<nb, kAdjPairBlock, 0, st>>>(P);
+      return cudaGetLastError();
+    }
+  }
   if (mrt)
     k_adjoint<St, true><<<nblk(A.s.g.n), 256, 0, st>>>(A);
   else

@@ -154,6 +154,16 @@ template <class Re> struct IsSingle {
 __host__ __device__ __forceinline__ float lbm_sqrt(float x) { return sqrtf(x); }
 __host__ __device__ __forceinline__ double lbm_sqrt(double x) { return sqrt(x); }
 
+// b > 0 ? a / b : 0, and "is any lane > 0" (a packed type overloads both).
+template <class Re>
+__host__ __device__ __forceinline__ Re div_if_pos(Re a, Re b) {
+  return b > Re(0) ? a / b : Re(0);
+}
+template <class Re>
+__host__ __device__ __forceinline__ bool any_pos(Re v) {
+  return v > Re(0);
+}
+
 // Derivative weight of clip(x, lo, hi) = min(max(x, lo), hi) under jax's
 // convention: 1 strictly inside, 1/2 at a tie with a bound, 0 outside.
 template <class Re>
@@ -657,12 +667,12 @@ __host__ __device__ __forceinline__ void collide_vjp_s(const CellScalars<Re>& cs
   if (smag) {
     // tau_eff = (tau + R)/2, R = sqrt(tau^2 + c pi inv_rr)
     const Re gR = Re(0.5) * g_tau_eff;
-    const Re gX = (R > Re(0)) ? gR / (Re(2) * R) : Re(0);
+    const Re gX = div_if_pos(gR, Re(2) * R);
     g_tau = Re(0.5) * g_tau_eff + gX * Re(2) * tau;
     const Re g_pi = gX * c18cs2 * inv_rr;
     const Re g_rho_direct = -gX * c18cs2 * pi * inv_rr * inv_rr;
-    if (pi > Re(0)) {
-      const Re ip = g_pi / pi;
+    if (any_pos(pi)) {
+      const Re ip = div_if_pos(g_pi, pi);
       Re gs[6];
       gs[0] = ip * sst[0];
       gs[1] = ip * sst[1];
