@@ -310,6 +310,70 @@ void lbm_xla_zou_he_inlet_vjp(void* stream, void** buffers, const char* opaque, 
 void lbm_xla_zou_he_outlet_vjp(void* stream, void** buffers, const char* opaque, size_t len);
 void lbm_xla_momentum_exchange_vjp(void* stream, void** buffers, const char* opaque, size_t len);
 
+/* ---- batched instances --------------------------------------------------
+ * Many independent sphere instances -- grids of different sizes, their own
+ * radius, q mode, porosity mode and sigmoid sharpness -- advanced by one kernel
+ * launch per step over all of them.  A gradient evaluation (forward with
+ * checkpoints, recompute, adjoint) and the optimiser step on every radius can
+ * run as one captured CUDA graph.  jax_lbm has no batched driver (its examples
+ * loop over configurations in Python, examples/11:197-225); these entry points
+ * have no counterpart there.  Instances use LBM_F32 storage and share the
+ * collision model and guard setting. */
+typedef struct lbm_batch lbm_batch;
+
+enum { LBM_LOSS_CD = 0, LBM_LOSS_TARGET_CD = 1 };
+
+/* optax.adam on the radius, then clip to [r_min, r_max] (examples/11:182-194).
+ * loss LBM_LOSS_CD minimises Cd (optim/losses.py minimize_cd_loss);
+ * LBM_LOSS_TARGET_CD minimises (Cd - target_cd)^2 (target_cd_loss). */
+typedef struct lbm_adam {
+  double lr;
+  double b1, b2, eps; /* optax defaults: 0.9, 0.999, 1e-8 */
+  double r_min, r_max;
+  int loss;
+  double target_cd;
+} lbm_adam;
+
+int lbm_batch_create(const lbm_params* params, int count, lbm_batch** out);
+int lbm_batch_destroy(lbm_batch* batch);
+int lbm_batch_size(lbm_batch* batch, int* count, long long* cells);
+/* The solver handle of instance i (owned by the batch), for per-instance
+ * queries such as lbm_get_state or lbm_get_projected_area. */
+int lbm_batch_instance(lbm_batch* batch, int i, lbm_sim** sim);
+/* One sphere per instance (spheres[count]); rebuilds each instance's geometry. */
+int lbm_batch_set_spheres(lbm_batch* batch, const lbm_sphere* spheres, void* stream);
+/* f_0 = f_eq(rho = 1, u = (inlet_velocity[0], 0, 0)) on every instance. */
+int lbm_batch_set_equilibrium(lbm_batch* batch, void* stream);
+int lbm_batch_set_state(lbm_batch* batch, int i, const void* f, void* stream);
+/* Advance every instance n_steps.  With sample_every > 0, samples (device,
+ * float64) receives [n_steps / sample_every][count][4] = (Fx, Fy, Fz, Cd). */
+int lbm_batched_run(lbm_batch* batch, int n_steps, int sample_every, double* samples,
+                    void* stream);
+/* Cd after n_steps and dCd/dr of every instance (host arrays [count]), from
+ * the initial state; checkpoint_every 0 picks the segment length from free
+ * device memory.  use_graph runs the evaluation as a captured CUDA graph
+ * (captured on first use, replayed while n_steps, the segment length and the
+ * block size stay the same). */
+int lbm_batch_cd_and_grad(lbm_batch* batch, int n_steps, int checkpoint_every, int use_graph,
+                          double* cd_host, double* dcd_dr_host, void* stream);
+/* n_iters optimisation iterations: gradient evaluation + Adam step on every
+ * radius (on the device, inside the graph with use_graph), then the geometry
+ * of the new radii.  Host histories [n_iters][count] (any may be NULL): the
+ * radius evaluated, the loss, Cd and dloss/dr. */
+int lbm_batch_optimize(lbm_batch* batch, int n_iters, int n_steps, int checkpoint_every,
+                       const lbm_adam* opt, int use_graph, double* r_hist, double* loss_hist,
+                       double* cd_hist, double* grad_hist, void* stream);
+int lbm_batch_get_radii(lbm_batch* batch, double* radii_host);
+/* Threads per block of the batched kernels: 128 or 256. */
+int lbm_batch_set_block(lbm_batch* batch, int block);
+/* Times a probe_steps gradient evaluation at each block size and keeps the
+ * faster; sets the checkpoint interval for n_steps to the longest segment the
+ * free device memory holds.  Returns both. */
+int lbm_batch_autotune(lbm_batch* batch, int probe_steps, int n_steps, int* block_out,
+                       int* checkpoint_out, void* stream);
+int lbm_batch_get_plan(lbm_batch* batch, int* block, int* segment_steps, int* recomputed_steps,
+                       unsigned long long* workspace_bytes, double* graph_build_seconds);
+
 #ifdef __cplusplus
 }
 #endif

@@ -13,6 +13,7 @@ from .core.equilibrium import compute_density, compute_velocity, equilibrium
 from .core.forces import drag_coefficient, momentum_exchange, projected_area
 from .core.lattice import CS2, D3Q19_OPPOSITE, D3Q19_VELOCITIES, D3Q19_WEIGHTS
 from .core.streaming import stream
+from .batch import Batch
 from .solver import Simulation
 from .state import LBMParams, LBMState, simulate, step
 
@@ -21,5 +22,5 @@ __all__ = [
     "equilibrium", "compute_density", "compute_velocity",
     "bgk", "mrt", "smagorinsky_tau", "stream", "zou_he_inlet", "zou_he_outlet",
     "momentum_exchange", "drag_coefficient", "projected_area",
-    "LBMState", "LBMParams", "step", "simulate", "Simulation",
+    "LBMState", "LBMParams", "step", "simulate", "Simulation", "Batch",
 ]

@@ -27,6 +27,7 @@ LBM_GUARD_OFF, LBM_GUARD_PRE, LBM_GUARD_POST = 0, 1, 2
 LBM_POROSITY_NONE, LBM_POROSITY_HARD, LBM_POROSITY_SOFT = 0, 1, 2
 LBM_Q_HALFWAY, LBM_Q_BOUZIDI = 0, 1
 LBM_SPHERE_DIST_MASK, LBM_SPHERE_SIGMOID_MASK = 0, 1
+LBM_LOSS_CD, LBM_LOSS_TARGET_CD = 0, 1
 
 
 class NativeLibraryMissing(RuntimeError):
@@ -74,6 +75,19 @@ class LBMSphereC(ctypes.Structure):
         ("porosity", ctypes.c_int),
         ("disc_floor", ctypes.c_double),
         ("denom_eps", ctypes.c_double),
+    ]
+
+
+class LBMAdamC(ctypes.Structure):
+    _fields_ = [
+        ("lr", ctypes.c_double),
+        ("b1", ctypes.c_double),
+        ("b2", ctypes.c_double),
+        ("eps", ctypes.c_double),
+        ("r_min", ctypes.c_double),
+        ("r_max", ctypes.c_double),
+        ("loss", ctypes.c_int),
+        ("target_cd", ctypes.c_double),
     ]
 
 
@@ -134,6 +148,23 @@ SIGNATURES = {
     "lbm_zou_he_outlet_vjp": [_i, _vp, _d, _vp, _vp, _vp, _i, _i, _i, _vp],
     "lbm_momentum_exchange_vjp": [_i, _vp, _vp, _vp, _vp, _i, _i, _i, _vp],
     "lbm_momentum_exchange_noalloc": [_i, _vp, _vp, _vp, _vp, _i, _i, _i, _vp],
+    # batched instances
+    "lbm_batch_create": [ctypes.POINTER(LBMParamsC), _i, ctypes.POINTER(_vp)],
+    "lbm_batch_destroy": [_vp],
+    "lbm_batch_size": [_vp, ctypes.POINTER(_i), ctypes.POINTER(_ll)],
+    "lbm_batch_instance": [_vp, _i, ctypes.POINTER(_vp)],
+    "lbm_batch_set_spheres": [_vp, ctypes.POINTER(LBMSphereC), _vp],
+    "lbm_batch_set_equilibrium": [_vp, _vp],
+    "lbm_batch_set_state": [_vp, _i, _vp, _vp],
+    "lbm_batched_run": [_vp, _i, _i, _vp, _vp],
+    "lbm_batch_cd_and_grad": [_vp, _i, _i, _i, ctypes.POINTER(_d), ctypes.POINTER(_d), _vp],
+    "lbm_batch_optimize": [_vp, _i, _i, _i, ctypes.POINTER(LBMAdamC), _i, ctypes.POINTER(_d),
+                           ctypes.POINTER(_d), ctypes.POINTER(_d), ctypes.POINTER(_d), _vp],
+    "lbm_batch_get_radii": [_vp, ctypes.POINTER(_d)],
+    "lbm_batch_set_block": [_vp, _i],
+    "lbm_batch_autotune": [_vp, _i, _i, ctypes.POINTER(_i), ctypes.POINTER(_i), _vp],
+    "lbm_batch_get_plan": [_vp, ctypes.POINTER(_i), ctypes.POINTER(_i), ctypes.POINTER(_i),
+                           ctypes.POINTER(ctypes.c_ulonglong), ctypes.POINTER(_d)],
 }
 _RESTYPES = {"lbm_status_string": ctypes.c_char_p, "lbm_last_error": ctypes.c_char_p}
 

@@ -23,7 +23,10 @@ LIBDIR = os.path.join(PKG, "lib")
 LIB = os.path.join(LIBDIR, "liblbm_gb300.so")
 
 ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]
+# host code: no a*b+c contraction, so host-side constants round the same on
+# x86-64 and aarch64 (where GCC would otherwise fuse them)
 NVCC_FLAGS = ["-std=c++17", "-O3", "-lineinfo", "-Xcompiler", "-fPIC", "-Xcompiler", "-O2",
+              "-Xcompiler", "-ffp-contract=off",
               "--expt-relaxed-constexpr", "-I" + INCLUDE, "-I" + CSRC]
 
 

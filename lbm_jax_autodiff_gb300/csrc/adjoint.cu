@@ -19,6 +19,7 @@
 //   dJ/dp   += mu_k . dB/dp  (sigmoid porosity, dp/dr = alpha p (1-p))
 //   dJ/dq   += nu_{k+1} . dT/dq (S_k), per wall link, times dq/dr
 //   lambda_k = C^T B^T mu_k;  nu_k = Z^T lambda_k on the inlet/outlet faces
+#include "batch.cuh"
 #include "capi_util.cuh"
 #include "sim.cuh"
 #include "vec2.cuh"
@@ -206,15 +207,17 @@ __device__ __forceinline__ void gather_mu(const AdjArgs<Re>& A, int idx, int x, 
 #define LBM_ADJ_MINB 3
 #endif
 
+// One block of the adjoint step: cells [block * blockDim.x, +blockDim.x);
+// the block's dJ/dr goes to gr_partials[block * 8 + warp].
 template <class St, bool MRT>
-__global__ void __launch_bounds__(256, sizeof(St) == 8 ? 1 : LBM_ADJ_MINB)
-    k_adjoint(const AdjArgs<typename Storage<St>::Re> A) {
+__device__ __forceinline__ void adjoint_body(const AdjArgs<typename Storage<St>::Re>& A,
+                                             int block) {
   using Re = typename Storage<St>::Re;
   using S = Storage<St>;
   const StepArgs<Re>& a = A.s;
   const Grid& g = a.g;
   const int n = g.n;
-  const int idx = blockIdx.x * blockDim.x + threadIdx.x;
+  const int idx = block * blockDim.x + threadIdx.x;
   const int fl = a.flags;
   double gr = 0.0;
 
@@ -307,7 +310,13 @@ __global__ void __launch_bounds__(256, sizeof(St) == 8 ? 1 : LBM_ADJ_MINB)
   // deterministic per-warp accumulation of dJ/dr across steps
 #pragma unroll
   for (int o = 16; o > 0; o >>= 1) gr += __shfl_down_sync(0xffffffffu, gr, o);
-  if ((threadIdx.x & 31) == 0) A.gr_partials[blockIdx.x * 8 + (threadIdx.x >> 5)] += gr;
+  if ((threadIdx.x & 31) == 0) A.gr_partials[block * 8 + (threadIdx.x >> 5)] += gr;
+}
+
+template <class St, bool MRT>
+__global__ void __launch_bounds__(256, sizeof(St) == 8 ? 1 : LBM_ADJ_MINB)
+    k_adjoint(const AdjArgs<typename Storage<St>::Re> A) {
+  adjoint_body<St, MRT>(A, blockIdx.x);
 }
 
 // ---------------------------------------------------------------------------
@@ -477,10 +486,10 @@ __global__ void __launch_bounds__(kAdjPairBlock, LBM_ADJ_PAIR_MINB)
 // nu_N = Z^T lambda_N with lambda_N = dJ/df_N from the momentum exchange:
 // lambda_N[opp j](x) = dJ/dFx * e_jx on every link (x, j).
 template <class Re>
-__global__ void k_adjoint_seed(StepArgs<Re> a, const double* __restrict__ dj_dfx,
-                               Re* __restrict__ nu) {
+__device__ __forceinline__ void adjoint_seed_cell(const StepArgs<Re>& a,
+                                                  const double* __restrict__ dj_dfx,
+                                                  Re* __restrict__ nu, int idx) {
   const Grid& g = a.g;
-  const int idx = blockIdx.x * blockDim.x + threadIdx.x;
   if (idx >= g.n) return;
   const size_t N = size_t(g.n);
   Re l[Q];
@@ -509,6 +518,12 @@ __global__ void k_adjoint_seed(StepArgs<Re> a, const double* __restrict__ dj_dfx
   }
 #pragma unroll
   for (int i = 0; i < Q; ++i) nu[i * N + idx] = l[i];
+}
+
+template <class Re>
+__global__ void k_adjoint_seed(StepArgs<Re> a, const double* __restrict__ dj_dfx,
+                               Re* __restrict__ nu) {
+  adjoint_seed_cell<Re>(a, dj_dfx, nu, blockIdx.x * blockDim.x + threadIdx.x);
 }
 
 // dJ/dFx = sign(Fx) / (0.5 rho U^2 A + 1e-10) from the finalized force record
@@ -602,6 +617,142 @@ cudaError_t launch_scatter_gq(const Grid& g, const uint32_t* tag, const LinkRec*
   k_scatter_gq<Re><<<nblk(g.n), 256, 0, st>>>(g, tag, rec, gq, out);
   return cudaGetLastError();
 }
+
+// ---------------------------------------------------------------------------
+// Batched forms: one launch covers every instance of a batch.
+// ---------------------------------------------------------------------------
+#ifndef LBM_ADJ_BATCH_MINB
+#define LBM_ADJ_BATCH_MINB 2
+#endif
+
+template <class St, bool MRT>
+__global__ void __launch_bounds__(256, LBM_ADJ_BATCH_MINB)
+    k_adjoint_batch(const AdjArgs<float>* __restrict__ args, const BatchInst* __restrict__ inst,
+                    const int2* __restrict__ map, int sprev_slot, int sk_slot, int nu_in_slot,
+                    int nu_out_slot, int first, int last) {
+  __shared__ AdjArgs<float> A;
+  const int2 m = map[blockIdx.x];
+  copy_to_shared(&A, args + m.x);
+  __syncthreads();
+  if (threadIdx.x == 0) {
+    const BatchInst& b = inst[m.x];
+    A.s.src = batch_slot(b, sprev_slot);
+    A.S_k = batch_slot(b, sk_slot);
+    A.nu_in = static_cast<const float*>(batch_slot(b, nu_in_slot));
+    A.nu_out = static_cast<float*>(batch_slot(b, nu_out_slot));
+    A.first = first;
+    A.last = last;
+    A.dj_dfx = b.out + 4;
+    A.gr_partials = b.gr_part;
+    A.gq = b.gq;
+  }
+  __syncthreads();
+  adjoint_body<St, MRT>(A, m.y);
+}
+
+__global__ void __launch_bounds__(256)
+    k_adjoint_seed_batch(const StepArgs<float>* __restrict__ args,
+                         const BatchInst* __restrict__ inst, const int2* __restrict__ map,
+                         int nu_slot) {
+  __shared__ StepArgs<float> sa;
+  const int2 m = map[blockIdx.x];
+  copy_to_shared(&sa, args + m.x);
+  __syncthreads();
+  const BatchInst& b = inst[m.x];
+  adjoint_seed_cell<float>(sa, b.out + 4, static_cast<float*>(batch_slot(b, nu_slot)),
+                           m.y * blockDim.x + threadIdx.x);
+}
+
+// Per instance (one block each): clear the dJ/dr partials and the per-link dJ/dq.
+__global__ void __launch_bounds__(256) k_zero_grad_batch(const BatchInst* __restrict__ inst) {
+  const BatchInst& b = inst[blockIdx.x];
+  for (int i = threadIdx.x; i < b.nblk * 8; i += blockDim.x) b.gr_part[i] = 0.0;
+  for (int i = threadIdx.x; i < b.ngq; i += blockDim.x) b.gq[i] = 0.0;
+}
+
+// Per instance (one block each): dCd/dr = fixed-order sum of the partials.
+__global__ void __launch_bounds__(256) k_reduce_gr_batch(const BatchInst* __restrict__ inst) {
+  __shared__ double sh[256];
+  const BatchInst& b = inst[blockIdx.x];
+  double v = 0.0;
+  for (int i = threadIdx.x; i < b.nblk * 8; i += blockDim.x) v += b.gr_part[i];
+  sh[threadIdx.x] = v;
+  __syncthreads();
+  for (int o = blockDim.x / 2; o > 0; o >>= 1) {
+    if (threadIdx.x < o) sh[threadIdx.x] += sh[threadIdx.x + o];
+    __syncthreads();
+  }
+  if (threadIdx.x == 0) b.out[5] = sh[0];
+}
+
+// One Adam step on each instance's radius (optax.adam, examples/11:182-194):
+// loss = Cd (minimize_cd_loss) or (Cd - target)^2 (target_cd_loss,
+// optim/losses.py:34-99); m, v bias-corrected; r clipped to [r_min, r_max]
+// afterwards.  opt[i] = (r, m, v, t).
+__global__ void k_adam_batch(const BatchInst* __restrict__ inst, int count, AdamP p,
+                             double* __restrict__ opt) {
+  const int i = blockIdx.x * blockDim.x + threadIdx.x;
+  if (i >= count) return;
+  const BatchInst& b = inst[i];
+  const double cd = b.out[3], dcd = b.out[5];
+  const double loss = p.target ? (cd - p.target_cd) * (cd - p.target_cd) : cd;
+  const double g = p.target ? 2.0 * (cd - p.target_cd) * dcd : dcd;
+  b.out[6] = loss;
+  b.out[7] = g;
+  double* o = opt + 4 * i;
+  const double t = o[3] + 1.0;
+  const double m = p.b1 * o[1] + (1.0 - p.b1) * g;
+  const double v = p.b2 * o[2] + (1.0 - p.b2) * g * g;
+  const double mh = m / (1.0 - pow(p.b1, t));
+  const double vh = v / (1.0 - pow(p.b2, t));
+  double r = o[0] - p.lr * mh / (sqrt(vh) + p.eps);
+  r = fmin(fmax(r, p.r_min), p.r_max);
+  o[0] = r;
+  o[1] = m;
+  o[2] = v;
+  o[3] = t;
+}
+
+template <class St>
+cudaError_t launch_adjoint_batch(const AdjArgs<float>* args, const BatchInst* inst,
+                                 const int2* map, int nblocks, int block, bool mrt,
+                                 int sprev_slot, int sk_slot, int nu_in_slot, int nu_out_slot,
+                                 int first, int last, cudaStream_t st) {
+  if (mrt)
+    k_adjoint_batch<St, true><<<nblocks, block, 0, st>>>(args, inst, map, sprev_slot, sk_slot,
+                                                        nu_in_slot, nu_out_slot, first, last);
+  else
+    k_adjoint_batch<St, false><<<nblocks, block, 0, st>>>(args, inst, map, sprev_slot, sk_slot,
+                                                         nu_in_slot, nu_out_slot, first, last);
+  return cudaGetLastError();
+}
+
+cudaError_t launch_adjoint_seed_batch(const StepArgs<float>* args, const BatchInst* inst,
+                                      const int2* map, int nblocks, int block, int nu_slot,
+                                      cudaStream_t st) {
+  k_adjoint_seed_batch<<<nblocks, block, 0, st>>>(args, inst, map, nu_slot);
+  return cudaGetLastError();
+}
+
+cudaError_t launch_zero_grad_batch(const BatchInst* inst, int count, cudaStream_t st) {
+  k_zero_grad_batch<<<count, 256, 0, st>>>(inst);
+  return cudaGetLastError();
+}
+
+cudaError_t launch_reduce_gr_batch(const BatchInst* inst, int count, cudaStream_t st) {
+  k_reduce_gr_batch<<<count, 256, 0, st>>>(inst);
+  return cudaGetLastError();
+}
+
+cudaError_t launch_adam_batch(const BatchInst* inst, int count, const AdamP& p, double* opt,
+                              cudaStream_t st) {
+  k_adam_batch<<<(count + 127) / 128, 128, 0, st>>>(inst, count, p, opt);
+  return cudaGetLastError();
+}
+
+template cudaError_t launch_adjoint_batch<float>(const AdjArgs<float>*, const BatchInst*,
+                                                 const int2*, int, int, bool, int, int, int, int,
+                                                 int, int, cudaStream_t);
 
 template cudaError_t launch_adjoint<float>(const AdjArgs<float>&, bool, cudaStream_t);
 template cudaError_t launch_adjoint<double>(const AdjArgs<double>&, bool, cudaStream_t);

@@ -322,8 +322,9 @@ __device__ __forceinline__ void pull_post_bc(const StepArgs<typename Storage<St>
   if (x == g.nx - 1 && !(a.flags & SF_NO_OUTLET)) zou_he_outlet<Re>(f, a.rho_out);
 }
 
-// Block-wide sum of three doubles; thread 0 writes them to out[blockIdx.x*3].
-__device__ __forceinline__ void block_sum3_store(double a, double b, double c, double* out) {
+// Block-wide sum of three doubles; thread 0 writes them to out[slot*3].
+__device__ __forceinline__ void block_sum3_store_at(double a, double b, double c, double* out,
+                                                    int slot) {
   __shared__ double sh[3][32];
 #pragma unroll
   for (int o = 16; o > 0; o >>= 1) {
@@ -346,11 +347,15 @@ __device__ __forceinline__ void block_sum3_store(double a, double b, double c, d
       c += __shfl_down_sync(0xffffffffu, c, o);
     }
     if (lane == 0) {
-      out[3 * blockIdx.x + 0] = a;
-      out[3 * blockIdx.x + 1] = b;
-      out[3 * blockIdx.x + 2] = c;
+      out[3 * slot + 0] = a;
+      out[3 * slot + 1] = b;
+      out[3 * slot + 2] = c;
     }
   }
+}
+
+__device__ __forceinline__ void block_sum3_store(double a, double b, double c, double* out) {
+  block_sum3_store_at(a, b, c, out, blockIdx.x);
 }
 
 }  // namespace lbm

@@ -24,18 +24,21 @@
 // storage; k_step serves FP32 / FP64, odd nz, the COLLIDE_ONLY / STREAM_ONLY
 // launches and the sampled steps that also sum the momentum-exchange force
 // (SF_FORCE).
+#include "batch.cuh"
 #include "sim.cuh"
 #include "vec2.cuh"
 
 namespace lbm {
 
+// One block of the fused step: cells [block * blockDim.x, +blockDim.x) of the
+// grid `a` describes; the force partial of the block goes to slot `block`.
 template <class St, bool MRT>
-__global__ void __launch_bounds__(256, sizeof(St) == 8 ? 2 : 4) k_step(const StepArgs<typename Storage<St>::Re> a) {
+__device__ __forceinline__ void step_body(const StepArgs<typename Storage<St>::Re>& a, int block) {
   using Re = typename Storage<St>::Re;
   using S = Storage<St>;
   const Grid& g = a.g;
   const int n = g.n;
-  const int idx = blockIdx.x * blockDim.x + threadIdx.x;
+  const int idx = block * blockDim.x + threadIdx.x;
   const int fl = a.flags;
   double fx = 0.0, fy = 0.0, fz = 0.0;
   unsigned resets = 0;
@@ -119,11 +122,16 @@ __global__ void __launch_bounds__(256, sizeof(St) == 8 ? 2 : 4) k_step(const Ste
     }
   }
 
-  if (fl & SF_FORCE) block_sum3_store(fx, fy, fz, a.force_partials);
+  if (fl & SF_FORCE) block_sum3_store_at(fx, fy, fz, a.force_partials, block);
   if ((fl & (SF_GUARD_PRE | SF_GUARD_POST)) && a.guard_count) {
     const unsigned tot = __reduce_add_sync(0xffffffffu, resets);
     if ((threadIdx.x & 31) == 0 && tot) atomicAdd(a.guard_count, (unsigned long long)tot);
   }
+}
+
+template <class St, bool MRT>
+__global__ void __launch_bounds__(256, sizeof(St) == 8 ? 2 : 4) k_step(const StepArgs<typename Storage<St>::Re> a) {
+  step_body<St, MRT>(a, blockIdx.x);
 }
 
 // Per-direction pointers of one pair launch: pull[i] + idx is the interior
@@ -340,6 +348,93 @@ cudaError_t launch_force_sum(const double* part, int nblocks, double* out3, cuda
   k_force_finalize<<<1, 256, 0, stream>>>(part, nblocks, 0.0, out3, 0);
   return cudaGetLastError();
 }
+
+// ---------------------------------------------------------------------------
+// Batched forms: one launch covers every instance of a batch.
+// ---------------------------------------------------------------------------
+template <class St, bool MRT>
+__global__ void __launch_bounds__(256, 4)
+    k_step_batch(const StepArgs<float>* __restrict__ args, const BatchInst* __restrict__ inst,
+                 const int2* __restrict__ map, int src_slot, int dst_slot, int extra_flags) {
+  __shared__ StepArgs<float> sa;
+  const int2 m = map[blockIdx.x];
+  copy_to_shared(&sa, args + m.x);
+  __syncthreads();
+  if (threadIdx.x == 0) {
+    const BatchInst& b = inst[m.x];
+    sa.src = batch_slot(b, src_slot);
+    sa.dst = batch_slot(b, dst_slot);
+    sa.flags |= extra_flags;
+    sa.force_partials = b.force_part;
+  }
+  __syncthreads();
+  step_body<St, MRT>(sa, m.y);
+}
+
+// Per instance (one block each): F from the block partials, Cd, and with
+// with_dj the objective's dJ/dFx = sign(Fx) / (0.5 rho U^2 A + 1e-10)
+// (forces.py:274-276).  With `samples`, (F, Cd) also go to samples[i*4..].
+__global__ void __launch_bounds__(256)
+    k_force_finalize_batch(const BatchInst* __restrict__ inst, int with_dj,
+                           double* __restrict__ samples) {
+  __shared__ double sh[3][256];
+  const BatchInst& b = inst[blockIdx.x];
+  double x = 0, y = 0, z = 0;
+  for (int i = threadIdx.x; i < b.nblk; i += blockDim.x) {
+    x += b.force_part[3 * i];
+    y += b.force_part[3 * i + 1];
+    z += b.force_part[3 * i + 2];
+  }
+  sh[0][threadIdx.x] = x;
+  sh[1][threadIdx.x] = y;
+  sh[2][threadIdx.x] = z;
+  __syncthreads();
+  for (int o = blockDim.x / 2; o > 0; o >>= 1) {
+    if (threadIdx.x < o) {
+      sh[0][threadIdx.x] += sh[0][threadIdx.x + o];
+      sh[1][threadIdx.x] += sh[1][threadIdx.x + o];
+      sh[2][threadIdx.x] += sh[2][threadIdx.x + o];
+    }
+    __syncthreads();
+  }
+  if (threadIdx.x == 0) {
+    const double fx = sh[0][0], den = *b.dyn_area + 1e-10;
+    b.out[0] = fx;
+    b.out[1] = sh[1][0];
+    b.out[2] = sh[2][0];
+    b.out[3] = fabs(fx) / den;
+    if (with_dj) b.out[4] = (fx > 0.0 ? 1.0 : (fx < 0.0 ? -1.0 : 0.0)) / den;
+    if (samples) {
+      samples[4 * blockIdx.x + 0] = fx;
+      samples[4 * blockIdx.x + 1] = sh[1][0];
+      samples[4 * blockIdx.x + 2] = sh[2][0];
+      samples[4 * blockIdx.x + 3] = fabs(fx) / den;
+    }
+  }
+}
+
+template <class St>
+cudaError_t launch_step_batch(const StepArgs<float>* args, const BatchInst* inst, const int2* map,
+                              int nblocks, int block, bool mrt, int src_slot, int dst_slot,
+                              int extra_flags, cudaStream_t stream) {
+  if (mrt)
+    k_step_batch<St, true><<<nblocks, block, 0, stream>>>(args, inst, map, src_slot, dst_slot,
+                                                         extra_flags);
+  else
+    k_step_batch<St, false><<<nblocks, block, 0, stream>>>(args, inst, map, src_slot, dst_slot,
+                                                          extra_flags);
+  return cudaGetLastError();
+}
+
+cudaError_t launch_force_finalize_batch(const BatchInst* inst, int count, int with_dj,
+                                        double* samples, cudaStream_t stream) {
+  k_force_finalize_batch<<<count, 256, 0, stream>>>(inst, with_dj, samples);
+  return cudaGetLastError();
+}
+
+template cudaError_t launch_step_batch<float>(const StepArgs<float>*, const BatchInst*,
+                                              const int2*, int, int, bool, int, int, int,
+                                              cudaStream_t);
 
 template cudaError_t launch_step<float>(const StepArgs<float>&, bool, cudaStream_t);
 template cudaError_t launch_step<double>(const StepArgs<double>&, bool, cudaStream_t);

@@ -39,6 +39,55 @@ def _require_cuda(t, name, dtype=None, numel=None):
         raise ValueError("%s must have %d elements, got %d" % (name, numel, t.numel()))
 
 
+def params_struct(nx, ny, nz, tau, collision="mrt", storage="fp32", use_smagorinsky=False,
+                  smagorinsky_cs=0.1, periodic_yz=True, guard="off",
+                  inlet_velocity=(0.05, 0.0, 0.0), rho_out=1.0, u_ref=None, area_min=1.0,
+                  exact_constants=False):
+    """lbm_params of one domain (validated)."""
+    if storage not in _STORAGE:
+        raise ValueError("storage must be one of %s" % sorted(_STORAGE))
+    if collision not in ("bgk", "mrt"):
+        raise ValueError("collision must be 'bgk' or 'mrt'")
+    if guard not in _GUARD:
+        raise ValueError("guard must be one of %s" % sorted(_GUARD))
+    inlet_velocity = tuple(float(v) for v in inlet_velocity)
+    p = nat.LBMParamsC()
+    p.nx, p.ny, p.nz = int(nx), int(ny), int(nz)
+    p.storage = _STORAGE[storage]
+    p.collision = nat.LBM_MRT if collision == "mrt" else nat.LBM_BGK
+    p.tau = float(tau)
+    p.use_smagorinsky = int(bool(use_smagorinsky))
+    p.smagorinsky_cs = float(smagorinsky_cs)
+    p.periodic_yz = int(bool(periodic_yz))
+    p.guard = _GUARD[guard]
+    for k in range(3):
+        p.inlet_velocity[k] = inlet_velocity[k]
+    p.rho_out = float(rho_out)
+    p.u_ref = float(u_ref if u_ref is not None else inlet_velocity[0])
+    p.area_min = float(area_min)
+    p.exact_constants = int(bool(exact_constants))
+    return p
+
+
+def sphere_struct(radius, center=(0.0, 0.0, 0.0), sharpness=20.0, kind="sigmoid",
+                  q_mode="bouzidi", porosity="hard", disc_floor=None, denom_eps=1e-20):
+    """lbm_sphere in the reference world frame (see Simulation.set_sphere)."""
+    s = nat.LBMSphereC()
+    for k in range(3):
+        s.center[k] = float(center[k])
+    s.radius = float(radius)
+    s.sharpness = float(sharpness)
+    s.kind = nat.LBM_SPHERE_SIGMOID_MASK if kind == "sigmoid" else nat.LBM_SPHERE_DIST_MASK
+    s.q_mode = nat.LBM_Q_BOUZIDI if q_mode == "bouzidi" else nat.LBM_Q_HALFWAY
+    s.porosity = {"none": nat.LBM_POROSITY_NONE, "hard": nat.LBM_POROSITY_HARD,
+                  "soft": nat.LBM_POROSITY_SOFT}[porosity]
+    if disc_floor is None:
+        disc_floor = 1e-10 if kind == "sigmoid" else 0.0
+    s.disc_floor = float(disc_floor)
+    s.denom_eps = float(denom_eps)
+    return s
+
+
 class Simulation:
     """One D3Q19 domain on the current CUDA device.
 
@@ -52,12 +101,9 @@ class Simulation:
                  inlet_velocity=(0.05, 0.0, 0.0), rho_out=1.0, u_ref=None, area_min=1.0,
                  exact_constants=False):
         nat.load()
-        if storage not in _STORAGE:
-            raise ValueError("storage must be one of %s" % sorted(_STORAGE))
-        if collision not in ("bgk", "mrt"):
-            raise ValueError("collision must be 'bgk' or 'mrt'")
-        if guard not in _GUARD:
-            raise ValueError("guard must be one of %s" % sorted(_GUARD))
+        p = params_struct(nx, ny, nz, tau, collision, storage, use_smagorinsky, smagorinsky_cs,
+                          periodic_yz, guard, inlet_velocity, rho_out, u_ref, area_min,
+                          exact_constants)
         self.shape = (int(nx), int(ny), int(nz))
         self.n = nx * ny * nz
         self.storage = storage
@@ -65,21 +111,6 @@ class Simulation:
         self.collision = collision
         self.tau = float(tau)
         self.inlet_velocity = tuple(float(v) for v in inlet_velocity)
-        p = nat.LBMParamsC()
-        p.nx, p.ny, p.nz = self.shape
-        p.storage = _STORAGE[storage]
-        p.collision = nat.LBM_MRT if collision == "mrt" else nat.LBM_BGK
-        p.tau = float(tau)
-        p.use_smagorinsky = int(bool(use_smagorinsky))
-        p.smagorinsky_cs = float(smagorinsky_cs)
-        p.periodic_yz = int(bool(periodic_yz))
-        p.guard = _GUARD[guard]
-        for k in range(3):
-            p.inlet_velocity[k] = self.inlet_velocity[k]
-        p.rho_out = float(rho_out)
-        p.u_ref = float(u_ref if u_ref is not None else self.inlet_velocity[0])
-        p.area_min = float(area_min)
-        p.exact_constants = int(bool(exact_constants))
         self._params = p
         self._h = ctypes.c_void_p()
         nat.call("lbm_create", ctypes.byref(p), ctypes.byref(self._h))
@@ -115,19 +146,8 @@ class Simulation:
         q_mode: "bouzidi" (ray-sphere q(r)) | "halfway" (q = 0.5).
         porosity: "hard" (bounce-back on solid cells) | "soft" (sigmoid blend).
         """
-        s = nat.LBMSphereC()
-        for k in range(3):
-            s.center[k] = float(center[k])
-        s.radius = float(radius)
-        s.sharpness = float(sharpness)
-        s.kind = nat.LBM_SPHERE_SIGMOID_MASK if kind == "sigmoid" else nat.LBM_SPHERE_DIST_MASK
-        s.q_mode = nat.LBM_Q_BOUZIDI if q_mode == "bouzidi" else nat.LBM_Q_HALFWAY
-        s.porosity = {"none": nat.LBM_POROSITY_NONE, "hard": nat.LBM_POROSITY_HARD,
-                      "soft": nat.LBM_POROSITY_SOFT}[porosity]
-        if disc_floor is None:
-            disc_floor = 1e-10 if kind == "sigmoid" else 0.0
-        s.disc_floor = float(disc_floor)
-        s.denom_eps = float(denom_eps)
+        s = sphere_struct(radius, center, sharpness, kind, q_mode, porosity, disc_floor,
+                          denom_eps)
         self.sphere = dict(radius=float(radius), center=tuple(center), sharpness=float(sharpness),
                            kind=kind, q_mode=q_mode, porosity=porosity)
         nat.call("lbm_set_geometry_sphere", self._h, ctypes.byref(s), _stream())
