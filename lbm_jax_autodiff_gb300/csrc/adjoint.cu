@@ -99,6 +99,7 @@ __device__ __forceinline__ double link_q_grad(const AdjArgs<typename Storage<St>
   const LinkRec& r = a.rec[ri - 1];
   const uint32_t lm = r.linkmask;
   const St* Sk = static_cast<const St*>(A.S_k);
+  const NearMask M(g, a.near, x, y, z, 1);
   double* gq = A.gq + size_t(ri - 1) * Q;
   double gr = 0.0;
 #pragma unroll
@@ -118,7 +119,7 @@ __device__ __forceinline__ double link_q_grad(const AdjArgs<typename Storage<St>
       } else {
         // b = 2 clip(q, 0, 0.5)
         const int nb = ahead_wrap(g, x, y, z, ex(i), ey(i), ez(i));
-        const Re s_nb = S::ld(Sk + io * N + nb, a.K.w[io]);
+        const Re s_nb = S::ld(Sk + io * N + nb, M.nbr_in(i) ? a.soff_near[io] : a.soff[io]);
         dout = clip_weight<Re>(qv, Re(0), Re(0.5)) * Re(2) * (s_io - s_nb);
       }
       const double gqv = double(nv) * double(dout);
@@ -321,7 +322,7 @@ __global__ void __launch_bounds__(256, sizeof(St) == 8 ? 1 : LBM_ADJ_MINB)
 
 // ---------------------------------------------------------------------------
 // k_adjoint_pair: the same adjoint step for two z-adjacent cells per thread
-// (FP32 arithmetic, nz even, no porosity blend): the interior gather of
+// (FP32 storage, nz even, no porosity blend): the interior gather of
 // nu_{k+1}, the recomputed f_k and the collision transpose run on packed
 // float2 values (FP32x2 pipe).  Pairs with a boundary record, on an x face or
 // on a non-periodic y/z edge take the per-cell path of k_adjoint lane by lane.
@@ -331,6 +332,7 @@ template <class St> struct AdjPairArgs {
   const St* pull[Q];      // S_{k-1} + i N - (e_x nyz + e_y nz + e_z): pull source of cell 0
   const float* push[Q];   // nu_{k+1} + j N + (e_x nyz + e_y nz + e_z): cell 0 + e_j
   float* out[Q];          // nu_k + i N
+  float2 soff2[2][Q];     // storage offsets outside / inside the body box (as PairArgs)
 };
 
 constexpr int kAdjPairBlock = 128;   // 256 cells per block, as k_adjoint
@@ -383,6 +385,8 @@ __global__ void __launch_bounds__(kAdjPairBlock, LBM_ADJ_PAIR_MINB)
     const uint32_t t1 = a.tag ? __ldg(a.tag + idx + 1) : 0u;
     bool special = ((t0 | t1) & TAG_INDEX) || x == 0 || x == g.nx - 1;
     if (!g.periodic_yz) special = special || y == 0 || y == g.ny - 1 || z == 0 || z + 2 == g.nz;
+    const int cls = near_class(g, a.near, x, y, z, 2);
+    special = special || cls == 2;
     V2 mu[Q], f[Q];
     if (!special) {
       const int nyz = g.ny * g.nz;
@@ -417,9 +421,10 @@ __global__ void __launch_bounds__(kAdjPairBlock, LBM_ADJ_PAIR_MINB)
         for (int i = 0; i < Q; ++i) {
           const int b = ey(i) == 1 ? iym : (ey(i) == -1 ? iyp : idx);
           const St* p = P.pull[i] + b;
-          if (ez(i) == 0) f[i] = Pr::ld2(p, K.w[i]);
-          else if (ez(i) == 1) f[i] = Pr::ld2s(p + zw0, p + 1, K.w[i]);
-          else f[i] = Pr::ld2s(p, p + 1 + zw1, K.w[i]);
+          const V2 so(P.soff2[cls][i]);
+          if (ez(i) == 0) f[i] = Pr::ld2(p, so);
+          else if (ez(i) == 1) f[i] = Pr::ld2s(p + zw0, p + 1, so);
+          else f[i] = Pr::ld2s(p, p + 1 + zw1, so);
         }
       }
     } else {
@@ -568,7 +573,10 @@ static inline int nblk(int n) { return (n + 255) / 256; }
 template <class St>
 cudaError_t launch_adjoint(const AdjArgs<typename Storage<St>::Re>& A, bool mrt,
                            cudaStream_t st) {
-  if constexpr (sizeof(typename Storage<St>::Re) == 4) {
+  // FP32 storage: the pair kernel (272 us vs 280 us per 256x128x128 step);
+  // 16-bit storage: the per-cell kernel (265 us vs 333 us -- the pair form
+  // spills once it also selects the storage offsets per class)
+  if constexpr (sizeof(St) == 4) {
     const Grid& g = A.s.g;
     if ((g.nz % 2) == 0 && !(A.s.flags & (SF_SOLID_SPHERE | SF_SOLID_FIELD))) {
       AdjPairArgs<St> P;
@@ -579,6 +587,8 @@ cudaError_t launch_adjoint(const AdjArgs<typename Storage<St>::Re>& A, bool mrt,
         P.pull[i] = static_cast<const St*>(A.s.src) + i * N - off;
         P.push[i] = A.nu_in + i * N + off;
         P.out[i] = A.nu_out + i * N;
+        P.soff2[0][i] = make_float2(A.s.soff[i], A.s.soff[i]);
+        P.soff2[1][i] = make_float2(A.s.soff_near[i], A.s.soff_near[i]);
       }
       const int nb = (g.n / 2 + kAdjPairBlock - 1) / kAdjPairBlock;
       if (mrt)

@@ -1,4 +1,5 @@
 // C ABI of the fused solver handle (include/lbm_gb300.h).
+#include <climits>
 #include <cstdio>
 #include <cstring>
 #include <string>
@@ -105,6 +106,8 @@ int finish_geometry(lbm_sim* s, const uint8_t* solid, const Re* q, const Re* dqd
                     cudaStream_t st) {
   int* counter = nullptr;
   int* cols = nullptr;
+  int* bb = nullptr;
+  int hbb[6] = {0, -1, 0, -1, 0, -1};
   const int ncol = s->g.ny * s->g.nz;
   LBM_TRY(dev_alloc((void**)&counter, sizeof(int)));
   if (!s->tag) LBM_TRY(dev_alloc((void**)&s->tag, s->n * sizeof(uint32_t)));
@@ -127,6 +130,19 @@ int finish_geometry(lbm_sim* s, const uint8_t* solid, const Re* q, const Re* dqd
                          "classify fill")))
       break;
     s->nrec = count;
+    // rest-offset box of 16-bit storage: the solid cells' bounding box grown
+    // by 2 cells (clipped to the grid)
+    if ((rc = dev_alloc((void**)&bb, 6 * sizeof(int)))) break;
+    {
+      const int init[6] = {INT_MAX, -1, INT_MAX, -1, INT_MAX, -1};
+      if ((rc = cuda_check(cudaMemcpyAsync(bb, init, sizeof(init), cudaMemcpyHostToDevice, st),
+                           "bbox H2D")))
+        break;
+      if ((rc = cuda_check(launch_solid_bbox(s->g, solid, bb, st), "bbox"))) break;
+      if ((rc = cuda_check(cudaMemcpyAsync(hbb, bb, sizeof(hbb), cudaMemcpyDeviceToHost, st),
+                           "bbox D2H")))
+        break;
+    }
     // link count and projected area
     if ((rc = dev_alloc((void**)&cols, ncol * sizeof(int)))) break;
     if ((rc = cuda_check(cudaMemsetAsync(cols, 0, ncol * sizeof(int), st), "memset"))) break;
@@ -145,6 +161,20 @@ int finish_geometry(lbm_sim* s, const uint8_t* solid, const Re* q, const Re* dqd
     long long a = 0;
     for (int v : hc) a += v;
     s->area = double(a);
+    if (hbb[1] < 0) {
+      for (int k = 0; k < 6; ++k) s->near[k] = 0;   // no solid: free-stream offset everywhere
+    } else {
+      const int dims[3] = {s->g.nx, s->g.ny, s->g.nz};
+      for (int k = 0; k < 3; ++k) {
+        int lo = hbb[2 * k] - 2, hi = hbb[2 * k + 1] + 3;
+        if (k == 2) {   // even z bounds: both cells of a z-pair share the class
+          lo &= ~1;
+          hi += hi & 1;
+        }
+        s->near[2 * k] = lo < 0 ? 0 : lo;
+        s->near[2 * k + 1] = hi > dims[k] ? dims[k] : hi;
+      }
+    }
     int nl = 0;
     for (const auto& r : hr) nl += __builtin_popcount(r.linkmask);
     s->nlinks = nl;
@@ -152,6 +182,7 @@ int finish_geometry(lbm_sim* s, const uint8_t* solid, const Re* q, const Re* dqd
   } while (0);
   cudaFree(counter);
   cudaFree(cols);
+  cudaFree(bb);
   return rc;
 }
 

@@ -220,6 +220,21 @@ __global__ void k_area_cols(Grid g, const uint8_t* __restrict__ solid, int* __re
   if (solid[idx] == 1) col[idx % (g.ny * g.nz)] = 1;
 }
 
+// Bounding box of the solid cells (any nonzero solid value): bb = {xmin,
+// xmax, ymin, ymax, zmin, zmax}, initialised by the caller to empty.
+__global__ void k_solid_bbox(Grid g, const uint8_t* __restrict__ solid, int* __restrict__ bb) {
+  const int idx = blockIdx.x * blockDim.x + threadIdx.x;
+  if (idx >= g.n || !solid[idx]) return;
+  int x, y, z;
+  decode(g, idx, x, y, z);
+  atomicMin(bb + 0, x);
+  atomicMax(bb + 1, x);
+  atomicMin(bb + 2, y);
+  atomicMax(bb + 3, y);
+  atomicMin(bb + 4, z);
+  atomicMax(bb + 5, z);
+}
+
 static inline int nblk(int n) { return (n + 255) / 256; }
 
 template <class Re>
@@ -264,6 +279,11 @@ cudaError_t launch_export_fields(const Grid& g, const SphereSpec& s, int with_po
                                  const uint8_t* solid, int32_t* solid_out, Re* porosity,
                                  cudaStream_t st) {
   k_export_fields<Re><<<nblk(g.n), 256, 0, st>>>(g, s, with_porosity, solid, solid_out, porosity);
+  return cudaGetLastError();
+}
+
+cudaError_t launch_solid_bbox(const Grid& g, const uint8_t* solid, int* bb, cudaStream_t st) {
+  k_solid_bbox<<<nblk(g.n), 256, 0, st>>>(g, solid, bb);
   return cudaGetLastError();
 }
 

@@ -81,7 +81,8 @@ __host__ __device__ constexpr bool is_conserved(int k) {
 
 // ---------------------------------------------------------------------------
 // Population storage.  FP32/FP64 store f itself; FP16/BF16 store the deviation
-// f_i - w_i from the rest weights (arithmetic stays FP32).
+// f_i - w from a per-direction offset w that the caller passes (the solver
+// uses the free-stream equilibrium); arithmetic stays FP32.
 // ---------------------------------------------------------------------------
 template <class St> struct Storage;
 template <> struct Storage<float> {

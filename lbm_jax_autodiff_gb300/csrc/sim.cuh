@@ -115,11 +115,68 @@ template <class Re> struct StepArgs {
   SphereP<Re> sph;
   const Re* porosity;     // [n]
   Re guard_reset[Q];
+  // 16-bit storage holds f_i minus an offset: the rest equilibrium w_i inside
+  // the box `near` around the body (where u ~ 0), the free-stream equilibrium
+  // f_eq(1, (u_in, 0, 0)) elsewhere -- so every cell stores a small deviation
+  Re soff[Q];             // outside the box
+  Re soff_near[Q];        // inside the box
+  int near[6];            // [x0, x1) x [y0, y1) x [z0, z1); empty when x0 >= x1
   double* force_partials; // [gridDim.x][3]
   unsigned long long* guard_count;
 };
 
 __device__ __forceinline__ int wrapi(int v, int n) { return v < 0 ? v + n : (v >= n ? v - n : v); }
+
+// ---- storage offsets of 16-bit populations ----------------------------------
+__device__ __forceinline__ bool in_near(const int b[6], int x, int y, int z) {
+  return x >= b[0] && x < b[1] && y >= b[2] && y < b[3] && z >= b[4] && z < b[5];
+}
+
+// In-box masks of a cell's neighbourhood, one bit per offset along each
+// axis: bit k of mx is "x + k - 1 inside the box" (x never wraps), of my
+// likewise with y wrapped, and of mz for z - 1 .. z + zc (wrapped), zc = 1
+// (one cell) or 2 (a z-pair).  The source x - e_i of direction i is inside
+// iff bit 1 - e_x of mx, 1 - e_y of my and 1 - e_z of mz are all set.
+struct NearMask {
+  unsigned mx, my, mz;
+  __device__ __forceinline__ NearMask(const Grid& g, const int b[6], int x, int y, int z, int zc) {
+    auto in = [](int v, int lo, int hi) { return unsigned(v >= lo && v < hi); };
+    mx = in(x - 1, b[0], b[1]) | (in(x, b[0], b[1]) << 1) | (in(x + 1, b[0], b[1]) << 2);
+    my = in(wrapi(y - 1, g.ny), b[2], b[3]) | (in(y, b[2], b[3]) << 1) |
+         (in(wrapi(y + 1, g.ny), b[2], b[3]) << 2);
+    mz = in(wrapi(z - 1, g.nz), b[4], b[5]) | (in(z, b[4], b[5]) << 1) |
+         (in(wrapi(z + 1, g.nz), b[4], b[5]) << 2);
+    if (zc == 2) mz |= in(wrapi(z + 2, g.nz), b[4], b[5]) << 3;
+  }
+  // 0: the whole neighbourhood outside, 1: inside, 2: mixed
+  __device__ __forceinline__ int cls(int zc) const {
+    const unsigned full_z = zc == 2 ? 15u : 7u;
+    if (mx == 0u || my == 0u || mz == 0u) return 0;
+    if (mx == 7u && my == 7u && mz == full_z) return 1;
+    return 2;
+  }
+  // class of the pull source x - e_i of the cell at z (lane 0)
+  __device__ __forceinline__ bool src_in(int i) const {
+    return ((mx >> (1 - ex(i))) & (my >> (1 - ey(i))) & (mz >> (1 - ez(i))) & 1u) != 0u;
+  }
+  // class of the neighbour x + e_i of the cell at z (lane 0)
+  __device__ __forceinline__ bool nbr_in(int i) const {
+    return ((mx >> (1 + ex(i))) & (my >> (1 + ey(i))) & (mz >> (1 + ez(i))) & 1u) != 0u;
+  }
+  __device__ __forceinline__ bool self_in() const { return ((mx & my & mz) >> 1) & 1u; }
+};
+
+__device__ __forceinline__ int near_class(const Grid& g, const int b[6], int x, int y, int z,
+                                          int zc) {
+  // x never wraps: most cells are decided by x alone
+  if (x + 1 < b[0] || x - 1 >= b[1]) return 0;
+  return NearMask(g, b, x, y, z, zc).cls(zc);
+}
+
+template <class Re>
+__device__ __forceinline__ Re soff_at(const StepArgs<Re>& a, int x, int y, int z, int i) {
+  return in_near(a.near, x, y, z) ? a.soff_near[i] : a.soff[i];
+}
 
 // Pull source of direction i for cell (x,y,z) following streaming.py:109-142:
 // x is never periodic, y/z are periodic or clamped; any out-of-range axis
@@ -278,31 +335,41 @@ __device__ __forceinline__ void pull_post_bc(const StepArgs<typename Storage<St>
   const Grid& g = a.g;
   const size_t N = size_t(g.n);
   const NbrOff O(g, x, y, z);
-  if (!O.face) {
+  // offset classes matter only for 16-bit storage (FP32/FP64 store f itself)
+  constexpr bool offs = sizeof(St) == 2;
+  const NearMask M(g, a.near, x, y, z, 1);
+  const int cls = offs ? M.cls(1) : 0;
+  if (!O.face && cls != 2) {
 #pragma unroll
-    for (int i = 0; i < Q; ++i) f[i] = S::ld(src + i * N + O.pull(i, idx), a.K.w[i]);
+    for (int i = 0; i < Q; ++i)
+      f[i] = S::ld(src + i * N + O.pull(i, idx), cls ? a.soff_near[i] : a.soff[i]);
   } else {
     const PullIdx P(g, x, y, z);
 #pragma unroll
-    for (int i = 0; i < Q; ++i) f[i] = S::ld(src + i * N + P.src(i, idx), a.K.w[i]);
+    for (int i = 0; i < Q; ++i) {
+      // offset class of the source cell (the cell itself on the fallback)
+      const bool in = P.valid(i) ? M.src_in(i) : M.self_in();
+      f[i] = S::ld(src + i * N + P.src(i, idx), in ? a.soff_near[i] : a.soff[i]);
+    }
   }
   const uint32_t ri = tag & TAG_INDEX;
   if (ri) {
     const LinkRec& r = a.rec[ri - 1];
     const uint32_t lm = r.linkmask;
+    const bool own_near = M.self_in();
 #pragma unroll
     for (int i = 1; i < Q; ++i) {
       const int io = opp(i);
       if (lm & (1u << io)) {
         const Re qv = Re(r.q[io]);
-        const Re s_opp = S::ld(src + io * N + idx, a.K.w[io]);
+        const Re s_opp = S::ld(src + io * N + idx, own_near ? a.soff_near[io] : a.soff[io]);
         if (qv >= Re(0.5)) {
-          const Re s_i = S::ld(src + i * N + idx, a.K.w[i]);
+          const Re s_i = S::ld(src + i * N + idx, own_near ? a.soff_near[i] : a.soff[i]);
           const Re inv2q = Re(1) / (Re(2) * fmin(qv, Re(1)));
           f[i] = inv2q * s_opp + (Re(1) - inv2q) * s_i;
         } else {
           const int nb = ahead_wrap(g, x, y, z, ex(i), ey(i), ez(i));
-          const Re s_nb = S::ld(src + io * N + nb, a.K.w[io]);
+          const Re s_nb = S::ld(src + io * N + nb, M.nbr_in(i) ? a.soff_near[io] : a.soff[io]);
           const Re twoq = Re(2) * fmax(qv, Re(0));
           f[i] = twoq * s_opp + (Re(1) - twoq) * s_nb;
         }

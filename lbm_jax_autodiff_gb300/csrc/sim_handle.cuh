@@ -38,6 +38,7 @@ cudaError_t launch_classify(const Grid& g, const uint8_t* solid, const Re* q, co
                             uint32_t* tag, LinkRec* rec, int cap, int* counter, int count_only,
                             cudaStream_t st);
 cudaError_t launch_area_cols(const Grid& g, const uint8_t* solid, int* col, cudaStream_t st);
+cudaError_t launch_solid_bbox(const Grid& g, const uint8_t* solid, int* bb, cudaStream_t st);
 template <class Re>
 cudaError_t launch_box_fields(const Grid& g, const double lo[3], const double hi[3],
                               uint8_t* solid, Re* q, cudaStream_t st);
@@ -87,6 +88,7 @@ struct lbm_sim {
   int nrec = 0;
   int nlinks = 0;
   double area = 0.0;
+  int near[6] = {0, 0, 0, 0, 0, 0};   // rest-offset box of 16-bit storage (solid bbox + 2)
   int have_geometry = 0;
   int porosity_mode = LBM_POROSITY_NONE;
   int sphere_porosity = 0;   // analytic sigmoid porosity in-kernel
@@ -157,6 +159,15 @@ inline void fill_args(const lbm_sim* s, StepArgs<Re>& a) {
   a.sph.sy = Re(s->g.ny / 4.0);
   a.sph.sz = Re(s->g.nz / 4.0);
   a.porosity = static_cast<const Re*>(s->porosity);
+  // 16-bit storage offsets: the rest equilibrium w inside the box around the
+  // body, the free-stream equilibrium f_eq(1, (U, 0, 0)) elsewhere
+  for (int i = 0; i < Q; ++i) {
+    const double U = s->p.inlet_velocity[0];
+    const double eu = ex(i) * U;
+    a.soff[i] = Re(double(a.K.w[i]) * (1.0 + 3.0 * eu + 4.5 * eu * eu - 1.5 * U * U));
+    a.soff_near[i] = a.K.w[i];
+  }
+  for (int k = 0; k < 6; ++k) a.near[k] = s->near[k];
   // guard reset targets: pre -> f_eq(1, (U,0,0)) (examples/10:160), post -> f_eq(1, 0) = w
   for (int i = 0; i < Q; ++i) {
     if (s->p.guard == LBM_GUARD_PRE) {

@@ -77,7 +77,8 @@ __device__ __forceinline__ void step_body(const StepArgs<typename Storage<St>::R
 #pragma unroll
         for (int j = 1; j < Q; ++j) {
           if (lm & (1u << j)) {
-            const double tot = double(S::ld(src + j * N + idx, a.K.w[j])) + double(f[opp(j)]);
+            const double tot =
+                double(S::ld(src + j * N + idx, soff_at(a, x, y, z, j))) + double(f[opp(j)]);
             fx += ex(j) * tot;
             fy += ey(j) * tot;
             fz += ez(j) * tot;
@@ -106,18 +107,21 @@ __device__ __forceinline__ void step_body(const StepArgs<typename Storage<St>::R
         collide_cell_rj<Re>(f, rho, jx, jy, jz, a.tau, MRT, (fl & SF_SMAG) != 0, a.c18cs2, a.K, c);
 
       St* dst = static_cast<St*>(a.dst);
+      const bool nr = in_near(a.near, x, y, z);
       if ((fl & SF_SOLID_HARD) && (tag & TAG_SOLID)) {
 #pragma unroll
-        for (int i = 0; i < Q; ++i) S::st(dst + i * N + idx, c[opp(i)], a.K.w[i]);
+        for (int i = 0; i < Q; ++i)
+          S::st(dst + i * N + idx, c[opp(i)], nr ? a.soff_near[i] : a.soff[i]);
       } else if (fl & (SF_SOLID_SPHERE | SF_SOLID_FIELD)) {
         const Re p = (fl & SF_SOLID_SPHERE) ? sphere_porosity<Re>(a.sph, x, y, z, nullptr)
                                             : a.porosity[idx];
         const Re omp = Re(1) - p;
 #pragma unroll
-        for (int i = 0; i < Q; ++i) S::st(dst + i * N + idx, omp * c[i] + p * c[opp(i)], a.K.w[i]);
+        for (int i = 0; i < Q; ++i)
+          S::st(dst + i * N + idx, omp * c[i] + p * c[opp(i)], nr ? a.soff_near[i] : a.soff[i]);
       } else {
 #pragma unroll
-        for (int i = 0; i < Q; ++i) S::st(dst + i * N + idx, c[i], a.K.w[i]);
+        for (int i = 0; i < Q; ++i) S::st(dst + i * N + idx, c[i], nr ? a.soff_near[i] : a.soff[i]);
       }
     }
   }
@@ -140,6 +144,9 @@ template <class St> struct PairArgs {
   StepArgs<float> a;
   const St* pull[Q];
   St* out[Q];
+  // storage offsets (both lanes): [0] outside the body box, [1] inside; the
+  // box's z bounds are even, so the two cells of a pair share the class
+  float2 soff2[2][Q];
 };
 
 constexpr int kPairBlock = 128;   // 256 cells per block
@@ -165,10 +172,11 @@ __device__ __forceinline__ unsigned guard_pair(V2 f[Q], V2& rho, V2& jx, V2& jy,
 // Smagorinsky + BGK/MRT collision on the FP32x2 pipe, hard bounce-back or
 // porosity blend, store of S_k through out[i] + idx.
 template <class St, bool MRT>
-__device__ __forceinline__ unsigned finish_pair(const StepArgs<float>& a, St* const* out, int idx,
-                                                int x, int y, int z, uint32_t t0, uint32_t t1,
-                                                V2 f[Q]) {
+__device__ __forceinline__ unsigned finish_pair(const PairArgs<St>& P, int idx, int x, int y,
+                                                int z, uint32_t t0, uint32_t t1, V2 f[Q]) {
   using Pr = Pair<St>;
+  const StepArgs<float>& a = P.a;
+  St* const* out = P.out;
   constexpr FixedConstsF K{};
   const int fl = a.flags;
   unsigned resets = 0;
@@ -181,12 +189,15 @@ __device__ __forceinline__ unsigned finish_pair(const StepArgs<float>& a, St* co
   V2 c[Q];
   collide_cell_rj<V2>(f, rho, jx, jy, jz, V2(a.tau), MRT, (fl & SF_SMAG) != 0, V2(a.c18cs2), K, c);
 
+  // storage offset class of the pair
+  const int nc = in_near(a.near, x, y, z) ? 1 : 0;
+  auto off = [&](int i) { return V2(P.soff2[nc][i]); };
   const bool s0 = (t0 & TAG_SOLID) != 0, s1 = (t1 & TAG_SOLID) != 0;
   if ((fl & SF_SOLID_HARD) && (s0 || s1)) {
 #pragma unroll
     for (int i = 0; i < Q; ++i)
       Pr::st2(out[i] + idx, V2(s0 ? c[opp(i)].x() : c[i].x(), s1 ? c[opp(i)].y() : c[i].y()),
-              K.w[i]);
+              off(i));
   } else if (fl & (SF_SOLID_SPHERE | SF_SOLID_FIELD)) {
     V2 p;
     if (fl & SF_SOLID_SPHERE)
@@ -196,10 +207,10 @@ __device__ __forceinline__ unsigned finish_pair(const StepArgs<float>& a, St* co
       p = V2(__ldg(reinterpret_cast<const float2*>(a.porosity + idx)));
     const V2 omp = V2(1.0f) - p;
 #pragma unroll
-    for (int i = 0; i < Q; ++i) Pr::st2(out[i] + idx, omp * c[i] + p * c[opp(i)], K.w[i]);
+    for (int i = 0; i < Q; ++i) Pr::st2(out[i] + idx, omp * c[i] + p * c[opp(i)], off(i));
   } else {
 #pragma unroll
-    for (int i = 0; i < Q; ++i) Pr::st2(out[i] + idx, c[i], K.w[i]);
+    for (int i = 0; i < Q; ++i) Pr::st2(out[i] + idx, c[i], off(i));
   }
   return resets;
 }
@@ -247,6 +258,8 @@ __global__ void __launch_bounds__(kPairBlock, 4) k_step_pair(const PairArgs<St> 
     const uint32_t t1 = a.tag ? __ldg(a.tag + idx + 1) : 0u;
     bool special = ((t0 | t1) & TAG_INDEX) || x == 0 || x == g.nx - 1;
     if (!g.periodic_yz) special = special || y == 0 || y == g.ny - 1 || z == 0 || z + 2 == g.nz;
+    const int cls = near_class(g, a.near, x, y, z, 2);
+    special = special || cls == 2;
     V2 f[Q];
     if (!special) {
       // interior pair: y wrap shared by both lanes, z wrap per lane
@@ -259,14 +272,15 @@ __global__ void __launch_bounds__(kPairBlock, 4) k_step_pair(const PairArgs<St> 
       for (int i = 0; i < Q; ++i) {
         const int b = ey(i) == 1 ? iym : (ey(i) == -1 ? iyp : idx);
         const St* p = P.pull[i] + b;
-        if (ez(i) == 0) f[i] = Pr::ld2(p, K.w[i]);
-        else if (ez(i) == 1) f[i] = Pr::ld2s(p + zw0, p + 1, K.w[i]);
-        else f[i] = Pr::ld2s(p, p + 1 + zw1, K.w[i]);
+        const V2 so(P.soff2[cls][i]);
+        if (ez(i) == 0) f[i] = Pr::ld2(p, so);
+        else if (ez(i) == 1) f[i] = Pr::ld2s(p + zw0, p + 1, so);
+        else f[i] = Pr::ld2s(p, p + 1 + zw1, so);
       }
     } else {
       pull_lanes<St>(a, idx, x, y, z, t0, t1, 3u, f);
     }
-    resets = finish_pair<St, MRT>(a, P.out, idx, x, y, z, t0, t1, f);
+    resets = finish_pair<St, MRT>(P, idx, x, y, z, t0, t1, f);
   }
   add_resets(a, resets);
 }
@@ -319,6 +333,8 @@ cudaError_t launch_step(const StepArgs<typename Storage<St>::Re>& a, bool mrt,
       for (int i = 0; i < Q; ++i) {
         P.pull[i] = static_cast<const St*>(a.src) + i * N - (ex(i) * nyz + ey(i) * g.nz + ez(i));
         P.out[i] = static_cast<St*>(a.dst) + i * N;
+        P.soff2[0][i] = make_float2(a.soff[i], a.soff[i]);
+        P.soff2[1][i] = make_float2(a.soff_near[i], a.soff_near[i]);
       }
       const int nb = (g.n / 2 + kPairBlock - 1) / kPairBlock;
       if (mrt)

@@ -77,60 +77,41 @@ template <> struct ScalarOf<V2> { using type = float; };
 // Populations of two z-adjacent cells (z even, z + 1) in the storage type.
 // ld2/st2 move the aligned pair at p (p even) as one 8-byte (FP32) or 4-byte
 // (FP16/BF16) access; ld2s gathers two separate elements.  16-bit storage
-// holds f - w, as Storage<> does.
+// holds f minus a per-direction offset w (one value per lane), as Storage<>
+// does.
 template <class St> struct Pair;
 template <> struct Pair<float> {
-  static __device__ __forceinline__ V2 ld2(const float* p, float) {
+  static __device__ __forceinline__ V2 ld2(const float* p, V2) {
     return V2(__ldg(reinterpret_cast<const float2*>(p)));
   }
-  static __device__ __forceinline__ V2 ld2s(const float* p0, const float* p1, float) {
+  static __device__ __forceinline__ V2 ld2s(const float* p0, const float* p1, V2) {
     return V2(__ldg(p0), __ldg(p1));
   }
-  static __device__ __forceinline__ void st2(float* p, V2 v, float) {
+  static __device__ __forceinline__ void st2(float* p, V2 v, V2) {
     *reinterpret_cast<float2*>(p) = v.v;
-  }
-  // shared-memory forms (plain loads)
-  static __device__ __forceinline__ V2 sh2(const float* p, float) {
-    return V2(*reinterpret_cast<const float2*>(p));
-  }
-  static __device__ __forceinline__ V2 sh2s(const float* p0, const float* p1, float) {
-    return V2(*p0, *p1);
   }
 };
 template <> struct Pair<__half> {
-  static __device__ __forceinline__ V2 ld2(const __half* p, float w) {
-    return V2(__half22float2(__ldg(reinterpret_cast<const __half2*>(p)))) + V2(w);
+  static __device__ __forceinline__ V2 ld2(const __half* p, V2 w) {
+    return V2(__half22float2(__ldg(reinterpret_cast<const __half2*>(p)))) + w;
   }
-  static __device__ __forceinline__ V2 ld2s(const __half* p0, const __half* p1, float w) {
-    return V2(__half22float2(__halves2half2(__ldg(p0), __ldg(p1)))) + V2(w);
+  static __device__ __forceinline__ V2 ld2s(const __half* p0, const __half* p1, V2 w) {
+    return V2(__half22float2(__halves2half2(__ldg(p0), __ldg(p1)))) + w;
   }
-  static __device__ __forceinline__ void st2(__half* p, V2 v, float w) {
-    *reinterpret_cast<__half2*>(p) = __float22half2_rn((v - V2(w)).v);
-  }
-  static __device__ __forceinline__ V2 sh2(const __half* p, float w) {
-    return V2(__half22float2(*reinterpret_cast<const __half2*>(p))) + V2(w);
-  }
-  static __device__ __forceinline__ V2 sh2s(const __half* p0, const __half* p1, float w) {
-    return V2(__half22float2(__halves2half2(*p0, *p1))) + V2(w);
+  static __device__ __forceinline__ void st2(__half* p, V2 v, V2 w) {
+    *reinterpret_cast<__half2*>(p) = __float22half2_rn((v - w).v);
   }
 };
 template <> struct Pair<__nv_bfloat16> {
-  static __device__ __forceinline__ V2 ld2(const __nv_bfloat16* p, float w) {
-    return V2(__bfloat1622float2(__ldg(reinterpret_cast<const __nv_bfloat162*>(p)))) + V2(w);
+  static __device__ __forceinline__ V2 ld2(const __nv_bfloat16* p, V2 w) {
+    return V2(__bfloat1622float2(__ldg(reinterpret_cast<const __nv_bfloat162*>(p)))) + w;
   }
   static __device__ __forceinline__ V2 ld2s(const __nv_bfloat16* p0, const __nv_bfloat16* p1,
-                                            float w) {
-    return V2(__bfloat1622float2(__halves2bfloat162(__ldg(p0), __ldg(p1)))) + V2(w);
+                                            V2 w) {
+    return V2(__bfloat1622float2(__halves2bfloat162(__ldg(p0), __ldg(p1)))) + w;
   }
-  static __device__ __forceinline__ void st2(__nv_bfloat16* p, V2 v, float w) {
-    *reinterpret_cast<__nv_bfloat162*>(p) = __float22bfloat162_rn((v - V2(w)).v);
-  }
-  static __device__ __forceinline__ V2 sh2(const __nv_bfloat16* p, float w) {
-    return V2(__bfloat1622float2(*reinterpret_cast<const __nv_bfloat162*>(p))) + V2(w);
-  }
-  static __device__ __forceinline__ V2 sh2s(const __nv_bfloat16* p0, const __nv_bfloat16* p1,
-                                            float w) {
-    return V2(__bfloat1622float2(__halves2bfloat162(*p0, *p1))) + V2(w);
+  static __device__ __forceinline__ void st2(__nv_bfloat16* p, V2 v, V2 w) {
+    *reinterpret_cast<__nv_bfloat162*>(p) = __float22bfloat162_rn((v - w).v);
   }
 };
 

@@ -92,7 +92,7 @@ class Simulation:
     """One D3Q19 domain on the current CUDA device.
 
     collision: "bgk" | "mrt"; storage: "fp32" | "fp64" | "fp16" | "bf16"
-    (16-bit storage keeps f_i - w_i, arithmetic in fp32); guard: "off" |
+    (16-bit storage keeps f_i - f_eq,i(1, (U, 0, 0)), arithmetic in fp32); guard: "off" |
     "pre" (examples/10:163-168) | "post" (state.py:161-169).
     """
 

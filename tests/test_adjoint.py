@@ -138,3 +138,24 @@ def test_guard_rejected(cuda):
     sim.set_state(sim.equilibrium_state())
     with pytest.raises(LBMError, match="UNSUPPORTED"):
         sim.cd_and_grad(4)
+
+
+@pytest.mark.parametrize("storage,cd_tol,g_tol", [("fp16", 1e-3, 1e-3), ("bf16", 3e-3, 3e-2)])
+def test_low_precision_gradient_vs_fp64(cuda, storage, cd_tol, g_tol):
+    """16-bit storage: Cd and dCd/dr against the FP64-storage solver on the
+    same problem (MRT + Smagorinsky, Bouzidi hard sphere, 400 steps)."""
+    nx, ny, nz, n = 64, 32, 32, 400
+    tau = 0.56
+
+    def run(st):
+        sim = _sim(nx, ny, nz, tau, storage=st, use_smagorinsky=True, smagorinsky_cs=0.1)
+        sim.set_sphere(0.5, kind="dist", q_mode="bouzidi", porosity="hard")
+        sim.set_state(sim.equilibrium_state())
+        out = sim.cd_and_grad(n, checkpoint_every=100)
+        sim.close()
+        return out
+
+    cd64, g64 = run("fp64")
+    cd, g = run(storage)
+    assert abs(cd - cd64) <= cd_tol * abs(cd64), (cd, cd64)
+    assert abs(g - g64) <= g_tol * abs(g64), (g, g64)

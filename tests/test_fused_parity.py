@@ -212,7 +212,8 @@ def test_fp64_mode_tight(cuda):
 
 @pytest.mark.parametrize("storage,tol", [("fp16", 2e-4), ("bf16", 2e-3)])
 def test_low_precision_storage(cuda, storage, tol):
-    """(f - w) in 16 bits, FP32 arithmetic: bounded deviation from FP32."""
+    """16-bit deviations (rest equilibrium near the body, free-stream
+    equilibrium elsewhere), FP32 arithmetic: bounded deviation from FP32."""
     nx, ny, nz = 48, 24, 24
     U = 0.05
     solid, q, _ = _oracle_sphere(nx, ny, nz, 0.5, (0.0, 0.0, 0.0), "sigmoid", "bouzidi", "hard",
