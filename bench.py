@@ -57,7 +57,7 @@ def _peaks():
 def _traffic_from_profiles(storage):
     """Per-launch DRAM bytes of the fused step from the committed ncu summary."""
     try:
-        with open(os.path.join(ROOT, "profiles", "roofline_traffic.json")) as fh:
+        with open(os.path.join(ROOT, "profiles", "k_step_fp32_256x128x128.traffic.json")) as fh:
             d = json.load(fh)
         return d.get(storage)
     except Exception:
@@ -147,26 +147,69 @@ def _oracle_step_sample(n_steps, threads):
     return dt, NX * NY * NZ * n_steps
 
 
+def _oracle_slab(planes, threads):
+    """An x-slab of `planes` planes of the bench workload for the CPU oracle:
+    the full-grid sphere geometry and initial state cut to x < planes (the
+    slab's first and last planes take the inlet / outlet rules)."""
+    import torch
+
+    from oracle import drivers, geometry
+    torch.set_num_threads(threads)
+    solid, q = geometry.create_sphere(NX, NY, NZ, (0.0, 0.0, 0.0), 0.5)
+    f = drivers.initial_state(NX, NY, NZ, U)
+    x0 = max(0, NX // 2 - planes // 2)
+    sl = slice(x0, x0 + planes)
+    cfg = drivers.StepConfig(tau=TAU, inlet=(U, 0.0, 0.0), collision="mrt", smagorinsky_cs=CS,
+                             guard="pre")
+    return (f[:, sl].contiguous(), q[:, sl].contiguous(), solid[sl].contiguous(), cfg)
+
+
 def run_reference(args):
+    """The CPU reference arm: W warm-up and K timed steps of the torch-CPU
+    restatement of jax_lbm on all host cores.  Each step is a bounded sample
+    of the workload -- one step on an x-slab of the 256x128x128 grid, the
+    slab sized from a calibration step so the whole run takes about 90 s."""
+    import torch
+
+    from oracle import drivers
     ws, rank, _ = _dist()
     if rank != 0:
         return 0
     threads = os.cpu_count() or 1
-    steps = max(1, args.steps_ref)
-    dt, updates = _oracle_step_sample(steps, threads)
-    mlups = updates / dt / 1e6
+    # calibrate: seconds per plane on a 32-plane slab (larger than the caches)
+    f, q, solid, cfg = _oracle_slab(32, threads)
+    with torch.no_grad():
+        drivers.step(f, q, cfg, solid=solid, f_ref=f)
+        t0 = time.perf_counter()
+        drivers.step(f, q, cfg, solid=solid, f_ref=f)
+        per_plane = (time.perf_counter() - t0) / 32
+    budget = 0.8 * 90.0 / (args.steps + args.warmup)
+    planes = int(min(NX, max(4, budget / per_plane)))
+    f, q, solid, cfg = _oracle_slab(planes, threads)
+    with torch.no_grad():
+        g = f
+        for _ in range(args.warmup):
+            g, _, _ = drivers.step(g, q, cfg, solid=solid, f_ref=f)
+        t0 = time.perf_counter()
+        for _ in range(args.steps):
+            g, _, _ = drivers.step(g, q, cfg, solid=solid, f_ref=f)
+        dt = time.perf_counter() - t0
+    cells = planes * NY * NZ
+    mlups = cells * args.steps / dt / 1e6
+    sample = ("per step: one step of an x-slab of %d of the 256 planes of the 256x128x128 "
+              "workload (%d cells) on the torch-CPU restatement of jax_lbm, %d threads"
+              % (planes, cells, threads))
     line = {
         "impl": "reference",
         "metric": "fwd MLUPS at 256x128x128 (MRT+Smagorinsky sphere step)",
         "value": round(mlups, 4), "unit": "MLUPS", "n_gpus": args.gpus,
-        "steps": steps, "warmup": 1, "ms_per_step": round(1e3 * dt / steps, 3),
+        "steps": args.steps, "warmup": args.warmup,
+        "ms_per_step": round(1e3 * dt / args.steps * NX / planes, 3),
         "higher_is_better": True, "scaling": "weak", "vs_baseline": None,
         "dtype": "f32", "data": "synthetic",
         "config": {"workload": WORKLOAD, "grid": [NX, NY, NZ]},
         "cpu_baseline": {"value": round(mlups, 4), "unit": "MLUPS", "cores": threads,
-                         "kind": "port",
-                         "sample": "%d step(s) of the full 256x128x128 workload, torch-CPU "
-                                   "restatement of jax_lbm, %d threads" % (steps, threads)},
+                         "kind": "port", "sample": sample},
         "e2e": {"value": round(mlups, 4), "unit": "MLUPS", "h2d_bytes_per_step": 0,
                 "d2h_bytes_per_step": 0},
     }
