@@ -91,12 +91,59 @@ void free_geometry(lbm_sim* s) {
   cudaFree(s->tag);
   cudaFree(s->rec);
   cudaFree(s->porosity);
+  cudaFree(s->spec_pairs);
+  cudaFree(s->spec_adj);
+  s->spec_pairs = s->spec_adj = nullptr;
+  s->nspec = s->nspec_adj = 0;
   s->tag = nullptr;
   s->rec = nullptr;
   s->porosity = nullptr;
   s->nrec = 0;
   s->nlinks = 0;
   s->have_geometry = 0;
+}
+
+// The pairs (z even) that the packed pair kernels run on their per-cell path,
+// in ascending order; flagged on the device with the kernels' own predicate.
+// Only for even nz (the pair kernels' condition).
+int build_pair_list(lbm_sim* s, cudaStream_t st) {
+  cudaFree(s->spec_pairs);
+  cudaFree(s->spec_adj);
+  s->spec_pairs = s->spec_adj = nullptr;
+  s->nspec = s->nspec_adj = 0;
+  if (s->g.nz % 2 != 0 || s->p.storage == LBM_F64) return LBM_OK;
+  const int np = s->g.n / 2;
+  const int use_class = (s->p.storage == LBM_F16 || s->p.storage == LBM_BF16) ? 1 : 0;
+  uint8_t* flags = nullptr;
+  LBM_TRY(dev_alloc((void**)&flags, size_t(np)));
+  std::vector<uint8_t> h(np);
+  int rc = cuda_check(launch_pair_flags(s->g, s->tag, s->near, use_class, flags, st), "pair flags");
+  if (!rc) rc = cuda_check(cudaMemcpyAsync(h.data(), flags, size_t(np), cudaMemcpyDeviceToHost, st),
+                           "flags D2H");
+  if (!rc) rc = cuda_check(cudaStreamSynchronize(st), "sync");
+  cudaFree(flags);
+  if (rc) return rc;
+  for (int which = 0; which < 2; ++which) {
+    std::vector<int> list;
+    for (int p = 0; p < np; ++p)
+      if (h[p] & (1u << which)) list.push_back(p);
+    int* d = nullptr;
+    LBM_TRY(dev_alloc((void**)&d, (list.empty() ? 1 : list.size()) * sizeof(int)));
+    if (!list.empty() &&
+        (rc = cuda_check(cudaMemcpy(d, list.data(), list.size() * sizeof(int),
+                                    cudaMemcpyHostToDevice), "list H2D"))) {
+      cudaFree(d);
+      return rc;
+    }
+    if (which == 0) {
+      s->spec_pairs = d;
+      s->nspec = int(list.size());
+    } else {
+      s->spec_adj = d;
+      s->nspec_adj = int(list.size());
+    }
+  }
+  return LBM_OK;
 }
 
 // Shared tail of the two geometry entry points: classify cells from the dense
@@ -178,6 +225,7 @@ int finish_geometry(lbm_sim* s, const uint8_t* solid, const Re* q, const Re* dqd
     int nl = 0;
     for (const auto& r : hr) nl += __builtin_popcount(r.linkmask);
     s->nlinks = nl;
+    if ((rc = build_pair_list(s, st))) break;
     s->have_geometry = 1;
   } while (0);
   cudaFree(counter);
@@ -474,8 +522,10 @@ int lbm_cd_and_grad(lbm_sim* s, int n_steps, int checkpoint_every, double* cd_ho
   const size_t state_bytes = s->n * Q * s->st_bytes;
   for (int b = 0; b < 2; ++b)
     if (!s->nu[b]) LBM_TRY(dev_alloc(&s->nu[b], s->n * Q * s->re_bytes));
+  // per-warp dJ/dr slots: nblocks * 8 of the step launches, then as many for
+  // the list launch of the pair kernels' boundary pairs
   if (!s->gr_partials)
-    LBM_TRY(dev_alloc((void**)&s->gr_partials, size_t(s->nblocks) * 8 * sizeof(double)));
+    LBM_TRY(dev_alloc((void**)&s->gr_partials, size_t(s->nblocks) * 16 * sizeof(double)));
   if (!s->scal) LBM_TRY(dev_alloc((void**)&s->scal, 8 * sizeof(double)));
   if (s->gq_cap < s->nrec) {
     cudaFree(s->gq);
@@ -543,7 +593,7 @@ int lbm_cd_and_grad(lbm_sim* s, int n_steps, int checkpoint_every, double* cd_ho
   LBM_TRY(cuda_check(launch_dj_dfx(s->scal, dyn_area(s), s->scal + 4, st), "dJ/dFx"));
 
   // ---- backward
-  LBM_TRY(cuda_check(cudaMemsetAsync(s->gr_partials, 0, size_t(s->nblocks) * 8 * sizeof(double), st), "memset"));
+  LBM_TRY(cuda_check(cudaMemsetAsync(s->gr_partials, 0, size_t(s->nblocks) * 16 * sizeof(double), st), "memset"));
   LBM_TRY(cuda_check(cudaMemsetAsync(s->gq, 0, size_t(s->gq_cap > 0 ? s->gq_cap : 1) * Q * sizeof(double), st), "memset"));
   int cur = 0;
   LBM_TRY(adjoint_seed(s, s->nu[cur], st));
@@ -565,7 +615,7 @@ int lbm_cd_and_grad(lbm_sim* s, int n_steps, int checkpoint_every, double* cd_ho
       cur = 1 - cur;
     }
   }
-  LBM_TRY(cuda_check(launch_reduce_sum(s->gr_partials, s->nblocks * 8, s->scal + 5, st), "reduce"));
+  LBM_TRY(cuda_check(launch_reduce_sum(s->gr_partials, s->nblocks * 16, s->scal + 5, st), "reduce"));
   if (dcd_dq) {
     cudaError_t e = is_fp64(s)
         ? launch_scatter_gq<double>(s->g, s->tag, s->rec, s->gq, static_cast<double*>(dcd_dq), st)

@@ -39,6 +39,8 @@ cudaError_t launch_classify(const Grid& g, const uint8_t* solid, const Re* q, co
                             cudaStream_t st);
 cudaError_t launch_area_cols(const Grid& g, const uint8_t* solid, int* col, cudaStream_t st);
 cudaError_t launch_solid_bbox(const Grid& g, const uint8_t* solid, int* bb, cudaStream_t st);
+cudaError_t launch_pair_flags(const Grid& g, const uint32_t* tag, const int near[6], int use_class,
+                              uint8_t* flags, cudaStream_t st);
 template <class Re>
 cudaError_t launch_box_fields(const Grid& g, const double lo[3], const double hi[3],
                               uint8_t* solid, Re* q, cudaStream_t st);
@@ -89,6 +91,10 @@ struct lbm_sim {
   int nlinks = 0;
   double area = 0.0;
   int near[6] = {0, 0, 0, 0, 0, 0};   // rest-offset box of 16-bit storage (solid bbox + 2)
+  int* spec_pairs = nullptr;          // pairs the forward pair kernel runs per cell
+  int nspec = 0;
+  int* spec_adj = nullptr;            // pairs the adjoint pair kernel runs per cell
+  int nspec_adj = 0;
   int have_geometry = 0;
   int porosity_mode = LBM_POROSITY_NONE;
   int sphere_porosity = 0;   // analytic sigmoid porosity in-kernel
@@ -168,6 +174,10 @@ inline void fill_args(const lbm_sim* s, StepArgs<Re>& a) {
     a.soff_near[i] = a.K.w[i];
   }
   for (int k = 0; k < 6; ++k) a.near[k] = s->near[k];
+  a.spec_pairs = s->spec_pairs;
+  a.spec_count = s->nspec;
+  a.spec_adj = s->spec_adj;
+  a.spec_adj_count = s->nspec_adj;
   // guard reset targets: pre -> f_eq(1, (U,0,0)) (examples/10:160), post -> f_eq(1, 0) = w
   for (int i = 0; i < Q; ++i) {
     if (s->p.guard == LBM_GUARD_PRE) {

@@ -241,48 +241,120 @@ __device__ __forceinline__ void add_resets(const StepArgs<float>& a, unsigned re
   }
 }
 
+// The boundary pairs (pair_special, listed in spec_pairs): the per-cell
+// pull with Bouzidi, Zou-He, fallback and per-direction storage offsets,
+// then the same packed collision and store.
 template <class St, bool MRT>
-__global__ void __launch_bounds__(kPairBlock, 4) k_step_pair(const PairArgs<St> P) {
-  using Pr = Pair<St>;
+__device__ __forceinline__ void step_pair_list_part(const PairArgs<St>& P, int nlist_block) {
   const StepArgs<float>& a = P.a;
   const Grid& g = a.g;
-  constexpr FixedConstsF K{};
-  const int pidx = blockIdx.x * blockDim.x + threadIdx.x;
+  const int t = nlist_block * blockDim.x + threadIdx.x;
   unsigned resets = 0;
-
-  if (pidx < (g.n >> 1)) {
-    const int idx = pidx << 1;
+  if (t < a.spec_count) {
+    const int idx = __ldg(a.spec_pairs + t) << 1;
     int x, y, z;
     decode(g, idx, x, y, z);
     const uint32_t t0 = a.tag ? __ldg(a.tag + idx) : 0u;
     const uint32_t t1 = a.tag ? __ldg(a.tag + idx + 1) : 0u;
-    bool special = ((t0 | t1) & TAG_INDEX) || x == 0 || x == g.nx - 1;
-    if (!g.periodic_yz) special = special || y == 0 || y == g.ny - 1 || z == 0 || z + 2 == g.nz;
-    const int cls = near_class(g, a.near, x, y, z, 2);
-    special = special || cls == 2;
     V2 f[Q];
-    if (!special) {
-      // interior pair: y wrap shared by both lanes, z wrap per lane
+    pull_lanes<St>(a, idx, x, y, z, t0, t1, 3u, f);
+    resets = finish_pair<St, MRT>(P, idx, x, y, z, t0, t1, f);
+  }
+  add_resets(a, resets);
+}
+
+// One launch in two parts: blocks [0, nlist) run the boundary pairs, the
+// rest the interior pairs (the list blocks first, so their longer latency
+// overlaps the interior blocks).
+template <class St, bool MRT>
+__global__ void __launch_bounds__(kPairBlock, 4) k_step_pair(const PairArgs<St> P, int nlist) {
+  using Pr = Pair<St>;
+  if (int(blockIdx.x) < nlist) {
+    step_pair_list_part<St, MRT>(P, blockIdx.x);
+    return;
+  }
+  const StepArgs<float>& a = P.a;
+  const Grid& g = a.g;
+  constexpr FixedConstsF K{};
+  const int pidx = (blockIdx.x - nlist) * blockDim.x + threadIdx.x;
+  unsigned resets = 0;
+
+  int idx = 0, x = 0, y = 0, z = 0;
+  uint32_t t0 = 0u, t1 = 0u;
+  bool active = pidx < (g.n >> 1);
+  if (active) {
+    idx = pidx << 1;
+    decode(g, idx, x, y, z);
+    t0 = a.tag ? __ldg(a.tag + idx) : 0u;
+    t1 = a.tag ? __ldg(a.tag + idx + 1) : 0u;
+    // boundary pairs run in k_step_pair_list
+    active = !pair_special(g, a.near, sizeof(St) == 2, false, x, y, z, t0, t1);
+  }
+  if (active) {
+    const int cls = sizeof(St) == 2 ? near_class(g, a.near, x, y, z, 2) : 0;
+    V2 f[Q];
+    {
+      // y wrap shared by both lanes, z wrap per lane; on the x faces the
+      // directions whose source lies outside keep the cell's own value
+      // (streaming.py:123-131)
       const int nyz = g.ny * g.nz;
       const int iym = idx + (y == 0 ? nyz : 0);          // e_y = +1 pulls y - 1
       const int iyp = idx - (y == g.ny - 1 ? nyz : 0);   // e_y = -1 pulls y + 1
       const int zw0 = z == 0 ? g.nz : 0;                 // lane 0, e_z = +1 pulls z - 1
       const int zw1 = z + 2 == g.nz ? -g.nz : 0;         // lane 1, e_z = -1 pulls z + 2
+      const int xlo = x == 0, xhi = x == g.nx - 1;
+      const size_t N = size_t(g.n);
 #pragma unroll
       for (int i = 0; i < Q; ++i) {
+        const V2 so(P.soff2[cls][i]);
+        if ((ex(i) == 1 && xlo) || (ex(i) == -1 && xhi)) {
+          f[i] = Pr::ld2(static_cast<const St*>(a.src) + i * N + idx, so);
+          continue;
+        }
         const int b = ey(i) == 1 ? iym : (ey(i) == -1 ? iyp : idx);
         const St* p = P.pull[i] + b;
-        const V2 so(P.soff2[cls][i]);
         if (ez(i) == 0) f[i] = Pr::ld2(p, so);
         else if (ez(i) == 1) f[i] = Pr::ld2s(p + zw0, p + 1, so);
         else f[i] = Pr::ld2s(p, p + 1 + zw1, so);
       }
-    } else {
-      pull_lanes<St>(a, idx, x, y, z, t0, t1, 3u, f);
+      if (xlo && !(a.flags & SF_NO_INLET)) {
+        V2 ux(a.u_in[0]), uy(a.u_in[1]), uz(a.u_in[2]);
+        if (a.flags & SF_INLET_FACE) {
+          const int fi = y * g.nz + z, fn = g.ny * g.nz;
+          ux = V2(a.u_face[fi], a.u_face[fi + 1]);
+          uy = V2(a.u_face[fn + fi], a.u_face[fn + fi + 1]);
+          uz = V2(a.u_face[2 * fn + fi], a.u_face[2 * fn + fi + 1]);
+        }
+        zou_he_inlet<V2>(f, ux, uy, uz);
+      }
+      if (xhi && !(a.flags & SF_NO_OUTLET)) zou_he_outlet<V2>(f, V2(a.rho_out));
     }
     resets = finish_pair<St, MRT>(P, idx, x, y, z, t0, t1, f);
   }
   add_resets(a, resets);
+}
+
+// Per pair: bit 0 if pair_special for the forward pair kernel, bit 1 for the
+// adjoint pair kernel (the kernels' own skip tests).
+__global__ void k_pair_flags(Grid g, const uint32_t* __restrict__ tag, Near nb, int use_class,
+                             uint8_t* __restrict__ flags) {
+  const int p = blockIdx.x * blockDim.x + threadIdx.x;
+  if (p >= (g.n >> 1)) return;
+  const int idx = p << 1;
+  int x, y, z;
+  decode(g, idx, x, y, z);
+  const uint32_t t0 = tag ? tag[idx] : 0u, t1 = tag ? tag[idx + 1] : 0u;
+  flags[p] = (pair_special(g, nb.b, use_class != 0, false, x, y, z, t0, t1) ? 1 : 0) |
+             (pair_special(g, nb.b, use_class != 0, true, x, y, z, t0, t1) ? 2 : 0);
+}
+
+cudaError_t launch_pair_flags(const Grid& g, const uint32_t* tag, const int near[6], int use_class,
+                              uint8_t* flags, cudaStream_t st) {
+  Near nb;
+  for (int k = 0; k < 6; ++k) nb.b[k] = near[k];
+  const int np = g.n >> 1;
+  k_pair_flags<<<(np + 255) / 256, 256, 0, st>>>(g, tag, nb, use_class, flags);
+  return cudaGetLastError();
 }
 
 // Deterministic reduction of the per-block force partials (fixed order) and
@@ -325,7 +397,8 @@ template <class St>
 cudaError_t launch_step(const StepArgs<typename Storage<St>::Re>& a, bool mrt,
                         cudaStream_t stream) {
   if constexpr (sizeof(St) == 2) {
-    if ((a.g.nz % 2) == 0 && !(a.flags & (SF_COLLIDE_ONLY | SF_STREAM_ONLY | SF_FORCE))) {
+    if ((a.g.nz % 2) == 0 && a.spec_pairs &&
+        !(a.flags & (SF_COLLIDE_ONLY | SF_STREAM_ONLY | SF_FORCE))) {
       PairArgs<St> P;
       P.a = a;
       const Grid& g = a.g;
@@ -337,10 +410,11 @@ cudaError_t launch_step(const StepArgs<typename Storage<St>::Re>& a, bool mrt,
         P.soff2[1][i] = make_float2(a.soff_near[i], a.soff_near[i]);
       }
       const int nb = (g.n / 2 + kPairBlock - 1) / kPairBlock;
+      const int nlist = (a.spec_count + kPairBlock - 1) / kPairBlock;
       if (mrt)
-        k_step_pair<St, true><<<nb, kPairBlock, 0, stream>>>(P);
+        k_step_pair<St, true><<<nlist + nb, kPairBlock, 0, stream>>>(P, nlist);
       else
-        k_step_pair<St, false><<<nb, kPairBlock, 0, stream>>>(P);
+        k_step_pair<St, false><<<nlist + nb, kPairBlock, 0, stream>>>(P, nlist);
       return cudaGetLastError();
     }
   }
