@@ -390,9 +390,9 @@ __global__ void k_force_finalize(const double* __restrict__ part, int nblocks, d
 }
 
 // FP32 storage runs k_step, the fastest form for it when measured at
-// 256x128x128 (114.6 us vs 118.7 us for k_step_pair); 16-bit storage runs
-// k_step_pair (102.4 us FP16 / 113.5 us BF16 vs 116.7 / 115.7 us), the pair
-// layout halving its conversion and address work per cell.
+// 256x128x128 (113-114 us vs 115-117 us for k_step_pair); 16-bit storage runs
+// k_step_pair (107-109 us vs ~117 us), the pair layout halving its
+// conversion and address work per cell.
 template <class St>
 cudaError_t launch_step(const StepArgs<typename Storage<St>::Re>& a, bool mrt,
                         cudaStream_t stream) {
