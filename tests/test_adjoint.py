@@ -159,3 +159,48 @@ def test_low_precision_gradient_vs_fp64(cuda, storage, cd_tol, g_tol):
     cd, g = run(storage)
     assert abs(cd - cd64) <= cd_tol * abs(cd64), (cd, cd64)
     assert abs(g - g64) <= g_tol * abs(g64), (g, g64)
+
+
+@pytest.mark.parametrize("nx,ny,nz,periodic,center", [
+    (32, 16, 16, False, (0.0, 0.0, 0.0)),     # pair kernel: non-periodic edges in its list
+    (33, 17, 15, True, (0.0, 0.0, 0.0)),      # odd nz: per-cell kernels
+    (32, 16, 16, True, (-2.6, 0.0, 0.0)),     # links next to the inlet face
+])
+def test_fp32_gradient_paths_vs_fp64_oracle(cuda, nx, ny, nz, periodic, center):
+    """FP32 storage dCd/dr through every adjoint path (packed interior pairs,
+    listed boundary pairs, per-cell kernels) within 1e-3 of the FP64 oracle."""
+    n, tau = 60, 0.56
+    dt = torch.float64
+    r = torch.tensor(0.5, dtype=dt, requires_grad=True)
+    cd = drivers.simulate_cd(r, nx, ny, nz, n, tau, q_mode="bouzidi", porosity_mode="hard",
+                             periodic_yz=periodic, center=center, dtype=dt,
+                             consts=consts_for(dt))
+    cd.backward()
+    sim = _sim(nx, ny, nz, tau, storage="fp32", periodic_yz=periodic)
+    sim.set_sphere(0.5, center=center, kind="sigmoid", q_mode="bouzidi", porosity="hard")
+    sim.set_state(sim.equilibrium_state())
+    cdg, gg = sim.cd_and_grad(n, checkpoint_every=20)
+    sim.close()
+    assert abs(cdg - cd.item()) <= 2e-4 * abs(cd.item()), (cdg, cd.item())
+    assert abs(gg - r.grad.item()) <= 1e-3 * abs(r.grad.item()), (gg, r.grad.item())
+
+
+@pytest.mark.parametrize("nx,ny,nz,periodic", [(48, 24, 24, False), (49, 25, 23, True)])
+def test_fp16_paths_vs_fp32(cuda, nx, ny, nz, periodic):
+    """FP16 storage through the pair kernels with a non-periodic box (edges
+    listed) and through the per-cell kernels (odd nz): Cd and dCd/dr within
+    the FP16 bar of the FP32 solver."""
+    n, tau = 200, 0.56
+
+    def run(st):
+        sim = _sim(nx, ny, nz, tau, storage=st, periodic_yz=periodic)
+        sim.set_sphere(0.5, kind="dist", q_mode="bouzidi", porosity="hard")
+        sim.set_state(sim.equilibrium_state())
+        out = sim.cd_and_grad(n, checkpoint_every=50)
+        sim.close()
+        return out
+
+    cd32, g32 = run("fp32")
+    cd16, g16 = run("fp16")
+    assert abs(cd16 - cd32) <= 1e-3 * abs(cd32), (cd16, cd32)
+    assert abs(g16 - g32) <= 1e-3 * abs(g32), (g16, g32)
