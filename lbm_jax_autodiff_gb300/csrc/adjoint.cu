@@ -637,8 +637,8 @@ __global__ void __launch_bounds__(256, LBM_ADJ_BATCH_MINB)
   const int2 m = map[blockIdx.x];
   copy_to_shared(&A, args + m.x);
   __syncthreads();
+  const BatchInst& b = inst[m.x];
   if (threadIdx.x == 0) {
-    const BatchInst& b = inst[m.x];
     A.s.src = batch_slot(b, sprev_slot);
     A.S_k = batch_slot(b, sk_slot);
     A.nu_in = static_cast<const float*>(batch_slot(b, nu_in_slot));
@@ -650,7 +650,8 @@ __global__ void __launch_bounds__(256, LBM_ADJ_BATCH_MINB)
     A.gq = b.gq;
   }
   __syncthreads();
-  adjoint_body<St, MRT>(A, m.y);
+  const int end = m.y + kBatchChunk < b.nblk ? m.y + kBatchChunk : b.nblk;
+  for (int sb = m.y; sb < end; ++sb) adjoint_body<St, MRT>(A, sb);
 }
 
 __global__ void __launch_bounds__(256)
@@ -662,8 +663,10 @@ __global__ void __launch_bounds__(256)
   copy_to_shared(&sa, args + m.x);
   __syncthreads();
   const BatchInst& b = inst[m.x];
-  adjoint_seed_cell<float>(sa, b.out + 4, static_cast<float*>(batch_slot(b, nu_slot)),
-                           m.y * blockDim.x + threadIdx.x);
+  float* nu = static_cast<float*>(batch_slot(b, nu_slot));
+  const int end = m.y + kBatchChunk < b.nblk ? m.y + kBatchChunk : b.nblk;
+  for (int sb = m.y; sb < end; ++sb)
+    adjoint_seed_cell<float>(sa, b.out + 4, nu, sb * blockDim.x + threadIdx.x);
 }
 
 // Per instance (one block each): clear the dJ/dr partials and the per-link dJ/dq.

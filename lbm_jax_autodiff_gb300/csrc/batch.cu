@@ -107,7 +107,7 @@ int build_map(lbm_batch* b) {
   std::vector<int2> map;
   for (int i : order) {
     const int nb = int((b->sims[i]->n + b->block - 1) / b->block);
-    for (int j = 0; j < nb; ++j) map.push_back(make_int2(i, j));
+    for (int j = 0; j < nb; j += kBatchChunk) map.push_back(make_int2(i, j));
   }
   cudaFree(b->d_map);
   b->d_map = nullptr;

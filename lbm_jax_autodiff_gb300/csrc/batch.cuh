@@ -1,7 +1,7 @@
 // Device-side tables of the batched solver: many independent instances
 // (grids of different sizes, own geometry and boundary modes) advanced by one
-// kernel launch per step.  Block b of a batched launch works on block
-// map[b].y of instance map[b].x; each instance's kernel arguments live in
+// kernel launch per step.  Block b of a batched launch works on sub-blocks
+// map[b].y .. map[b].y + kBatchChunk - 1 of instance map[b].x; each instance's kernel arguments live in
 // device memory, so a launch captured in a CUDA graph stays valid when the
 // host rebuilds an instance's geometry between replays.
 #pragma once
@@ -15,6 +15,11 @@ namespace lbm {
 // ping-pong states), SLOT_NU0 / SLOT_NU1 (adjoint states), and j >= 0 for
 // workspace state j (checkpoints, then the recompute stash).
 enum : int { SLOT_F0 = -1, SLOT_S0 = -2, SLOT_S1 = -3, SLOT_NU0 = -4, SLOT_NU1 = -5 };
+
+// Sub-blocks (one block's worth of cells each) that one block of a batched
+// launch walks after staging its instance's arguments once: map[b].y is the
+// first of them.
+constexpr int kBatchChunk = 4;
 
 struct BatchInst {
   void* f0;

@@ -450,15 +450,16 @@ __global__ void __launch_bounds__(256, 4)
   const int2 m = map[blockIdx.x];
   copy_to_shared(&sa, args + m.x);
   __syncthreads();
+  const BatchInst& b = inst[m.x];
   if (threadIdx.x == 0) {
-    const BatchInst& b = inst[m.x];
     sa.src = batch_slot(b, src_slot);
     sa.dst = batch_slot(b, dst_slot);
     sa.flags |= extra_flags;
     sa.force_partials = b.force_part;
   }
   __syncthreads();
-  step_body<St, MRT>(sa, m.y);
+  const int end = m.y + kBatchChunk < b.nblk ? m.y + kBatchChunk : b.nblk;
+  for (int sb = m.y; sb < end; ++sb) step_body<St, MRT>(sa, sb);
 }
 
 // Per instance (one block each): F from the block partials, Cd, and with
