@@ -155,6 +155,18 @@ template <class Re> struct IsSingle {
 __host__ __device__ __forceinline__ float lbm_sqrt(float x) { return sqrtf(x); }
 __host__ __device__ __forceinline__ double lbm_sqrt(double x) { return sqrt(x); }
 
+// Output sink of the collision routines: an array (out[i] = v) or a callable
+// out(i, v) that consumes each post-collision population as it is produced
+// (a kernel that stores them straight away holds no output array).
+template <class Re>
+__host__ __device__ __forceinline__ void emit(Re* out, int i, Re v) {
+  out[i] = v;
+}
+template <class F, class Re>
+__host__ __device__ __forceinline__ auto emit(F& out, int i, Re v) -> decltype(out(i, v), void()) {
+  out(i, v);
+}
+
 // b > 0 ? a / b : 0, and "is any lane > 0" (a packed type overloads both).
 template <class Re>
 __host__ __device__ __forceinline__ Re div_if_pos(Re a, Re b) {
@@ -310,9 +322,9 @@ __host__ __device__ __forceinline__ void mrt_moments(const Re f[Q], Re m[Q]) {
   m[18] = jz_xz - jz_yz;
 }
 
-// out_i = in_i - sum_{k non-conserved} M[k][i] d_k
-template <class Re>
-__host__ __device__ __forceinline__ void mrt_back(const Re d[Q], const Re in[Q], Re out[Q]) {
+// out_i = in_i - sum_{k non-conserved} M[k][i] d_k (out may alias in)
+template <class Re, class Out>
+__host__ __device__ __forceinline__ void mrt_back(const Re d[Q], const Re in[Q], Out out) {
   const Re cf = Re(-11) * d[1] - Re(4) * d[2];
   const Re ce = Re(8) * d[1] + d[2];
   const Re fx = Re(2) * d[9] - Re(4) * d[10];
@@ -321,34 +333,34 @@ __host__ __device__ __forceinline__ void mrt_back(const Re d[Q], const Re in[Q],
   const Re exy = ce + d[9] + d[10] + d[11] + d[12];
   const Re exz = ce + d[9] + d[10] - d[11] - d[12];
   const Re eyz = ce - Re(2) * (d[9] + d[10]);
-  out[0] = in[0] - (Re(-30) * d[1] + Re(12) * d[2]);
-  out[1] = in[1] - (cf + fx - Re(4) * d[4]);
-  out[2] = in[2] - (cf + fx + Re(4) * d[4]);
-  out[3] = in[3] - (cf + fy - Re(4) * d[6]);
-  out[4] = in[4] - (cf + fy + Re(4) * d[6]);
-  out[5] = in[5] - (cf + fz - Re(4) * d[8]);
-  out[6] = in[6] - (cf + fz + Re(4) * d[8]);
+  emit(out, 0, in[0] - (Re(-30) * d[1] + Re(12) * d[2]));
+  emit(out, 1, in[1] - (cf + fx - Re(4) * d[4]));
+  emit(out, 2, in[2] - (cf + fx + Re(4) * d[4]));
+  emit(out, 3, in[3] - (cf + fy - Re(4) * d[6]));
+  emit(out, 4, in[4] - (cf + fy + Re(4) * d[6]));
+  emit(out, 5, in[5] - (cf + fz - Re(4) * d[8]));
+  emit(out, 6, in[6] - (cf + fz + Re(4) * d[8]));
   // xy edges: rows 4, 6, 13, 16, 17
   const Re a46p = d[4] + d[6], a46m = d[4] - d[6];
   const Re b1617p = d[16] + d[17], b1617m = d[16] - d[17];
-  out[7] = in[7] - (exy + a46p + d[13] + b1617m);
-  out[8] = in[8] - (exy - a46m - d[13] - b1617p);
-  out[9] = in[9] - (exy + a46m - d[13] + b1617p);
-  out[10] = in[10] - (exy - a46p + d[13] - b1617m);
+  emit(out, 7, in[7] - (exy + a46p + d[13] + b1617m));
+  emit(out, 8, in[8] - (exy - a46m - d[13] - b1617p));
+  emit(out, 9, in[9] - (exy + a46m - d[13] + b1617p));
+  emit(out, 10, in[10] - (exy - a46p + d[13] - b1617m));
   // xz edges: rows 4, 8, 15, 16, 18
   const Re a48p = d[4] + d[8], a48m = d[4] - d[8];
   const Re b1618p = d[16] + d[18], b1618m = d[16] - d[18];
-  out[11] = in[11] - (exz + a48p + d[15] - b1618m);
-  out[12] = in[12] - (exz - a48m - d[15] + b1618p);
-  out[13] = in[13] - (exz + a48m - d[15] - b1618p);
-  out[14] = in[14] - (exz - a48p + d[15] + b1618m);
+  emit(out, 11, in[11] - (exz + a48p + d[15] - b1618m));
+  emit(out, 12, in[12] - (exz - a48m - d[15] + b1618p));
+  emit(out, 13, in[13] - (exz + a48m - d[15] - b1618p));
+  emit(out, 14, in[14] - (exz - a48p + d[15] + b1618m));
   // yz edges: rows 6, 8, 14, 17, 18
   const Re a68p = d[6] + d[8], a68m = d[6] - d[8];
   const Re b1718p = d[17] + d[18], b1718m = d[17] - d[18];
-  out[15] = in[15] - (eyz + a68p + d[14] + b1718m);
-  out[16] = in[16] - (eyz - a68m - d[14] - b1718p);
-  out[17] = in[17] - (eyz + a68m - d[14] + b1718p);
-  out[18] = in[18] - (eyz - a68p + d[14] - b1718m);
+  emit(out, 15, in[15] - (eyz + a68p + d[14] + b1718m));
+  emit(out, 16, in[16] - (eyz - a68m - d[14] - b1718p));
+  emit(out, 17, in[17] - (eyz + a68m - d[14] + b1718p));
+  emit(out, 18, in[18] - (eyz - a68p + d[14] - b1718m));
 }
 
 // Equilibrium moments (lattice.py:342-391) for the non-conserved rows.
@@ -474,19 +486,19 @@ __host__ __device__ __forceinline__ Re smag_tau(Re tau, Re c18cs2, Re pi, Re inv
 // Collision forward.  ``omega`` = 1 / tau_eff.  BGK: f - omega (f - f_eq).
 // MRT: f - M^-1 S (M f - m_eq), with S = rates and omega in the stress slots.
 // ---------------------------------------------------------------------------
-template <class Re, class W>
+template <class Re, class W, class Out>
 __host__ __device__ __forceinline__ void bgk_collide(const Re f[Q], Re rho, Re ux, Re uy, Re uz,
-                                            Re omega, const W& w, Re out[Q]) {
+                                            Re omega, const W& w, Out out) {
   Re feq[Q];
   equilibrium<Re>(rho, ux, uy, uz, w, feq);
 #pragma unroll
-  for (int i = 0; i < Q; ++i) out[i] = f[i] - omega * (f[i] - feq[i]);
+  for (int i = 0; i < Q; ++i) emit(out, i, Re(f[i] - omega * (f[i] - feq[i])));
 }
 
-template <class Re, class RT>
+template <class Re, class RT, class Out>
 __host__ __device__ __forceinline__ void mrt_relax_back(const Re f[Q], const Re m[Q], Re rho,
                                                         Re ux, Re uy, Re uz, Re omega,
-                                                        const RT& rate, Re out[Q]) {
+                                                        const RT& rate, Out out) {
   using Sc = typename ScalarOf<Re>::type;
   Re meq[Q], d[Q];
   mrt_meq<Re>(rho, ux, uy, uz, meq);
@@ -502,9 +514,9 @@ __host__ __device__ __forceinline__ void mrt_relax_back(const Re f[Q], const Re 
   mrt_back<Re>(d, f, out);
 }
 
-template <class Re, class RT>
+template <class Re, class RT, class Out>
 __host__ __device__ __forceinline__ void mrt_collide(const Re f[Q], Re rho, Re ux, Re uy, Re uz,
-                                            Re omega, const RT& rate, Re out[Q]) {
+                                            Re omega, const RT& rate, Out out) {
   Re m[Q];
   mrt_moments<Re>(f, m);
   mrt_relax_back<Re>(f, m, rho, ux, uy, uz, omega, rate, out);
@@ -512,10 +524,10 @@ __host__ __device__ __forceinline__ void mrt_collide(const Re f[Q], Re rho, Re u
 
 // Full collide of one cell given its density and momentum: optional
 // Smagorinsky tau, then BGK/MRT.  Returns omega actually used.
-template <class Re, class KT>
+template <class Re, class KT, class Out>
 __host__ __device__ __forceinline__ Re collide_cell_rj(const Re f[Q], Re rho, Re jx, Re jy, Re jz,
                                                        Re tau, bool mrt, bool smag, Re c18cs2,
-                                                       const KT& K, Re out[Q]) {
+                                                       const KT& K, Out out) {
   const Re ir = Re(1) / rho;
   const Re ux = jx * ir, uy = jy * ir, uz = jz * ir;
   Re omega;
@@ -546,9 +558,9 @@ __host__ __device__ __forceinline__ Re collide_cell_rj(const Re f[Q], Re rho, Re
   return omega;
 }
 
-template <class Re, class KT>
+template <class Re, class KT, class Out>
 __host__ __device__ __forceinline__ Re collide_cell(const Re f[Q], Re tau, bool mrt, bool smag,
-                                                    Re c18cs2, const KT& K, Re out[Q]) {
+                                                    Re c18cs2, const KT& K, Out out) {
   Re jx, jy, jz;
   momentum<Re>(f, jx, jy, jz);
   return collide_cell_rj<Re>(f, density<Re>(f), jx, jy, jz, tau, mrt, smag, c18cs2, K, out);
