@@ -566,6 +566,54 @@ __host__ __device__ __forceinline__ Re collide_cell(const Re f[Q], Re tau, bool 
   return collide_cell_rj<Re>(f, density<Re>(f), jx, jy, jz, tau, mrt, smag, c18cs2, K, out);
 }
 
+// g_i += c0 + e_i . h (+ sum_ab e_ia e_ib q_ab when Quad, q = xx, yy, zz, xy,
+// xz, yz with the off-diagonal terms already doubled).  Opposite directions
+// share the even part and take the odd part with opposite signs.
+template <class Re, bool Quad>
+__host__ __device__ __forceinline__ void cell_terms_add(Re g[Q], Re c0, Re hx, Re hy, Re hz,
+                                                        const Re q[6]) {
+  g[0] += c0;
+  const Re ax = Quad ? Re(c0 + q[0]) : c0;
+  const Re ay = Quad ? Re(c0 + q[1]) : c0;
+  const Re az = Quad ? Re(c0 + q[2]) : c0;
+  g[1] += ax + hx;
+  g[2] += ax - hx;
+  g[3] += ay + hy;
+  g[4] += ay - hy;
+  g[5] += az + hz;
+  g[6] += az - hz;
+  // xy edges: 7 (1,1,0), 10 (-1,-1,0), 9 (1,-1,0), 8 (-1,1,0)
+  {
+    const Re b = Quad ? Re(ax + q[1]) : c0;
+    const Re p = Quad ? Re(b + q[3]) : c0, m = Quad ? Re(b - q[3]) : c0;
+    const Re s = hx + hy, d = hx - hy;
+    g[7] += p + s;
+    g[10] += p - s;
+    g[9] += m + d;
+    g[8] += m - d;
+  }
+  // xz edges: 11 (1,0,1), 14 (-1,0,-1), 13 (1,0,-1), 12 (-1,0,1)
+  {
+    const Re b = Quad ? Re(ax + q[2]) : c0;
+    const Re p = Quad ? Re(b + q[4]) : c0, m = Quad ? Re(b - q[4]) : c0;
+    const Re s = hx + hz, d = hx - hz;
+    g[11] += p + s;
+    g[14] += p - s;
+    g[13] += m + d;
+    g[12] += m - d;
+  }
+  // yz edges: 15 (0,1,1), 18 (0,-1,-1), 17 (0,1,-1), 16 (0,-1,1)
+  {
+    const Re b = Quad ? Re(ay + q[2]) : c0;
+    const Re p = Quad ? Re(b + q[5]) : c0, m = Quad ? Re(b - q[5]) : c0;
+    const Re s = hy + hz, d = hy - hz;
+    g[15] += p + s;
+    g[18] += p - s;
+    g[17] += m + d;
+    g[16] += m - d;
+  }
+}
+
 // ---------------------------------------------------------------------------
 // Collision VJP.  The pre-collision populations enter only through a few
 // per-cell scalars (rho, u and the raw second moments, which also give the
@@ -672,47 +720,43 @@ __host__ __device__ __forceinline__ void collide_vjp_s(const CellScalars<Re>& cs
 #pragma unroll
     for (int i = 0; i < Q; ++i) g[i] *= (Re(1) - omega);
   }
-  macro_vjp_add<Re>(grho, gx, gy, gz, rho, ux, uy, uz, g);
-
   // omega = 1 / tau_eff
   const Re g_tau_eff = -g_omega * omega * omega;
   Re g_tau = g_tau_eff;
+  Re gs[6];
+  bool quad = false;
   if (smag) {
     // tau_eff = (tau + R)/2, R = sqrt(tau^2 + c pi inv_rr)
     const Re gR = Re(0.5) * g_tau_eff;
     const Re gX = div_if_pos(gR, Re(2) * R);
     g_tau = Re(0.5) * g_tau_eff + gX * Re(2) * tau;
     const Re g_pi = gX * c18cs2 * inv_rr;
-    const Re g_rho_direct = -gX * c18cs2 * pi * inv_rr * inv_rr;
+    // d(inv_rr)/d rho, the same for every population
+    grho += -gX * c18cs2 * pi * inv_rr * inv_rr;
     if (any_pos(pi)) {
       const Re ip = div_if_pos(g_pi, pi);
-      Re gs[6];
       gs[0] = ip * sst[0];
       gs[1] = ip * sst[1];
       gs[2] = ip * sst[2];
       gs[3] = Re(2) * ip * sst[3];
       gs[4] = Re(2) * ip * sst[4];
       gs[5] = Re(2) * ip * sst[5];
-      // s = p(f) - eq(rho, u): direct part through the raw moments p
-#pragma unroll
-      for (int i = 0; i < Q; ++i) {
-        const int x = ex(i), y = ey(i), z = ez(i);
-        Re t = Re(0);
-        if (x != 0) t += gs[0];
-        if (y != 0) t += gs[1];
-        if (z != 0) t += gs[2];
-        if (x * y != 0) t += Re(x * y) * gs[3];
-        if (x * z != 0) t += Re(x * z) * gs[4];
-        if (y * z != 0) t += Re(y * z) * gs[5];
-        g[i] += t;
-      }
+      // s = p(f) - eq(rho, u): the equilibrium part goes through rho and u,
+      // the raw moments p add e_ia e_ib gs_ab per population (below)
       Re er, exx, eyy, ezz;
       eq_second_vjp<Re>(K.w, rho, ux, uy, uz, gs, er, exx, eyy, ezz);
-      macro_vjp_add<Re>(-er, -exx, -eyy, -ezz, rho, ux, uy, uz, g);
+      grho -= er;
+      gx -= exx;
+      gy -= eyy;
+      gz -= ezz;
+      quad = true;
     }
-#pragma unroll
-    for (int i = 0; i < Q; ++i) g[i] += g_rho_direct;
   }
+  // rho = sum f, u = sum e f / rho: g_i += grho + (e_i - u) . g_u / rho
+  const Re hx = gx * ir, hy = gy * ir, hz = gz * ir;
+  const Re c0 = grho - (hx * ux + hy * uy + hz * uz);
+  if (quad) cell_terms_add<Re, true>(g, c0, hx, hy, hz, gs);
+  else cell_terms_add<Re, false>(g, c0, hx, hy, hz, gs);
   if (g_tau_out) *g_tau_out = g_tau;
 }
 
