@@ -91,6 +91,16 @@ template <> struct Pair<float> {
     *reinterpret_cast<float2*>(p) = v.v;
   }
 };
+// float(h) + c for a bfloat16 h in one mixed-precision add (sm_100+); the
+// conversion is exact, so this rounds as convert-then-add does.  (Measured
+// 98 us against 104 us per bf16 step at 256x128x128; for fp16 storage the
+// plain convert-then-add form measured faster.)
+__device__ __forceinline__ float add_bf16(__nv_bfloat16 h, float c) {
+  float d;
+  asm("add.rn.f32.bf16 %0, %1, %2;" : "=f"(d) : "h"(__bfloat16_as_ushort(h)), "f"(c));
+  return d;
+}
+
 template <> struct Pair<__half> {
   static __device__ __forceinline__ V2 ld2(const __half* p, V2 w) {
     return V2(__half22float2(__ldg(reinterpret_cast<const __half2*>(p)))) + w;
@@ -104,11 +114,12 @@ template <> struct Pair<__half> {
 };
 template <> struct Pair<__nv_bfloat16> {
   static __device__ __forceinline__ V2 ld2(const __nv_bfloat16* p, V2 w) {
-    return V2(__bfloat1622float2(__ldg(reinterpret_cast<const __nv_bfloat162*>(p)))) + w;
+    const __nv_bfloat162 v = __ldg(reinterpret_cast<const __nv_bfloat162*>(p));
+    return V2(add_bf16(__low2bfloat16(v), w.x()), add_bf16(__high2bfloat16(v), w.y()));
   }
   static __device__ __forceinline__ V2 ld2s(const __nv_bfloat16* p0, const __nv_bfloat16* p1,
                                             V2 w) {
-    return V2(__bfloat1622float2(__halves2bfloat162(__ldg(p0), __ldg(p1)))) + w;
+    return V2(add_bf16(__ldg(p0), w.x()), add_bf16(__ldg(p1), w.y()));
   }
   static __device__ __forceinline__ void st2(__nv_bfloat16* p, V2 v, V2 w) {
     *reinterpret_cast<__nv_bfloat162*>(p) = __float22bfloat162_rn((v - w).v);
