@@ -250,7 +250,12 @@ __device__ __forceinline__ double adjoint_cell(const AdjArgs<typename Storage<St
         p = sphere_porosity<Re>(a.sph, x, y, z, &dpdr);
       else
         p = a.porosity[idx];
-      if (ri || (fl & SF_SOLID_SPHERE)) {
+      // dJ/dr gets mu . dB/dp dp/dr; dp/dr = alpha p (1 - p) is below
+      // alpha 2^-40 (2^-70 in FP64) outside a shell a few cells thick around
+      // the surface, 4e-12 of its peak alpha / 4, so the collision recompute
+      // is skipped there
+      const Re tiny = sizeof(Re) == 8 ? Re(8.470329472543003e-22) : Re(9.094947017729282e-13);
+      if (ri || ((fl & SF_SOLID_SPHERE) && dpdr > a.sph.alpha * tiny)) {
         // dJ/dp = mu . (c[opp] - c) with c = C(f_k)
         Re c[Q];
         collide_cell<Re>(f, a.tau, MRT, (fl & SF_SMAG) != 0, a.c18cs2, a.K, c);
