@@ -352,20 +352,51 @@ constexpr int kAdjPairBlock = 128;   // 256 cells per block, as k_adjoint
 #define LBM_ADJ_PAIR_MINB 4
 #endif
 
-// The part of a pair's adjoint step after mu and f_k: hard-wall B^T,
-// lambda_k = C^T mu on the packed values, Zou-He transposes on the faces,
-// store of nu_k.
-template <class St, bool MRT>
-__device__ __forceinline__ void adj_pair_finish(const AdjPairArgs<St>& P, int idx, int x, int y,
-                                                int z, uint32_t t0, uint32_t t1, V2 mu[Q],
-                                                V2 f[Q]) {
+// The part of a pair's adjoint step after mu and f_k: the transpose B^T of
+// the hard bounce-back or (SOFT) of the porosity blend, with dJ/dp for a
+// sigmoid sphere; lambda_k = C^T mu on the packed values; Zou-He transposes
+// on the faces; store of nu_k.  Returns the pair's dJ/dr contribution
+// (nonzero only for a sigmoid sphere).
+template <class St, bool MRT, bool SOFT>
+__device__ __forceinline__ double adj_pair_finish(const AdjPairArgs<St>& P, int idx, int x, int y,
+                                                  int z, uint32_t t0, uint32_t t1, V2 mu[Q],
+                                                  V2 f[Q]) {
   const AdjArgs<float>& A = P.A;
   const StepArgs<float>& a = A.s;
   const Grid& g = a.g;
   constexpr FixedConstsF K{};
   const int fl = a.flags;
-  // B^T of the hard bounce-back: S_i = c_opp(i) on solid cells
-  if (fl & SF_SOLID_HARD) {
+  double gr = 0.0;
+  if constexpr (SOFT) {
+    // S = (1 - p) c + p c_opp per lane (smooth.py:118-155).  A sigmoid
+    // sphere adds dJ/dr += mu . (c_opp - c) dp/dr, skipped where dp/dr <
+    // alpha 2^-40 as in adjoint_cell
+    V2 p;
+    if (fl & SF_SOLID_SPHERE) {
+      float d0, d1;
+      p = V2(sphere_porosity<float>(a.sph, x, y, z, &d0),
+             sphere_porosity<float>(a.sph, x, y, z + 1, &d1));
+      const float thr = a.sph.alpha * 9.094947017729282e-13f;
+      const bool n0 = d0 > thr, n1 = d1 > thr;
+      if (n0 || n1) {
+        // mu . (c_opp - c) = sum_i c_i (mu_opp(i) - mu_i), summed as C emits c_i
+        V2 gp(0.0f);
+        auto acc = [&](int i, V2 c) { gp = gp + c * (mu[opp(i)] - mu[i]); };
+        collide_cell<V2>(f, V2(a.tau), MRT, (fl & SF_SMAG) != 0, V2(a.c18cs2), K, acc);
+        if (n0) gr += double(gp.x()) * double(d0);
+        if (n1) gr += double(gp.y()) * double(d1);
+      }
+    } else {
+      p = V2(__ldg(reinterpret_cast<const float2*>(a.porosity + idx)));
+    }
+    const V2 omp = V2(1.0f) - p;
+    V2 m2[Q];
+#pragma unroll
+    for (int i = 0; i < Q; ++i) m2[i] = omp * mu[i] + p * mu[opp(i)];
+#pragma unroll
+    for (int i = 0; i < Q; ++i) mu[i] = m2[i];
+  } else if (fl & SF_SOLID_HARD) {
+    // B^T of the hard bounce-back: S_i = c_opp(i) on solid cells
     const bool s0 = (t0 & TAG_SOLID) != 0, s1 = (t1 & TAG_SOLID) != 0;
     if (s0 || s1) {
       V2 m2[Q];
@@ -397,9 +428,11 @@ __device__ __forceinline__ void adj_pair_finish(const AdjPairArgs<St>& P, int id
   }
 #pragma unroll
   for (int i = 0; i < Q; ++i) *reinterpret_cast<float2*>(P.out[i] + idx) = mu[i].v;
+  return gr;
 }
 
-// One launch in two parts.  Blocks [0, nlist): the boundary pairs
+
+// k_adjoint_pair is one launch in two parts.  Blocks [0, nlist): the boundary pairs
 // (pair_special, listed in spec_pairs), one thread per cell on the per-cell
 // adjoint of k_adjoint, dJ/dr partials after the per-cell slots.  Blocks
 // [nlist, ...): the interior pairs on packed values.  The list blocks come
@@ -421,25 +454,23 @@ __device__ __forceinline__ void adjoint_pair_list_part(const AdjPairArgs<St>& P,
                   (threadIdx.x >> 5)] += gr;
 }
 
-template <class St, bool MRT>
-__global__ void __launch_bounds__(kAdjPairBlock, LBM_ADJ_PAIR_MINB)
-    k_adjoint_pair(const AdjPairArgs<St> P, int nlist) {
+// One interior pair of interior block `iblock`: mu_k gathered from
+// nu_{k+1}, f_k pulled from S_{k-1}, then adj_pair_finish.  Returns the
+// pair's dJ/dr contribution.
+template <class St, bool MRT, bool SOFT>
+__device__ __forceinline__ double adjoint_pair_interior(const AdjPairArgs<St>& P, int iblock) {
   using Pr = Pair<St>;
-  if (int(blockIdx.x) < nlist) {
-    adjoint_pair_list_part<St, MRT>(P, blockIdx.x);
-    return;
-  }
   const AdjArgs<float>& A = P.A;
   const StepArgs<float>& a = A.s;
   const Grid& g = a.g;
-  const int pidx = (blockIdx.x - nlist) * blockDim.x + threadIdx.x;
-  if (pidx >= (g.n >> 1)) return;
+  const int pidx = iblock * blockDim.x + threadIdx.x;
+  if (pidx >= (g.n >> 1)) return 0.0;
   const int idx = pidx << 1;
   int x, y, z;
   decode(g, idx, x, y, z);
   const uint32_t t0 = a.tag ? __ldg(a.tag + idx) : 0u;
   const uint32_t t1 = a.tag ? __ldg(a.tag + idx + 1) : 0u;
-  if (pair_special(g, a.near, sizeof(St) == 2, true, x, y, z, t0, t1)) return;
+  if (pair_special(g, a.near, sizeof(St) == 2, true, x, y, z, t0, t1)) return 0.0;
   const int cls = sizeof(St) == 2 ? near_class(g, a.near, x, y, z, 2) : 0;
   V2 mu[Q], f[Q];
   const int nyz = g.ny * g.nz;
@@ -481,7 +512,31 @@ __global__ void __launch_bounds__(kAdjPairBlock, LBM_ADJ_PAIR_MINB)
       else f[i] = Pr::ld2s(p, p + 1 + zw1, so);
     }
   }
-  adj_pair_finish<St, MRT>(P, idx, x, y, z, t0, t1, mu, f);
+  return adj_pair_finish<St, MRT, SOFT>(P, idx, x, y, z, t0, t1, mu, f);
+}
+
+
+// Interior block `iblock`; a sigmoid sphere's dJ/dr partials go to the
+// per-cell slots gr_partials[iblock * 8 + warp] (256 cells per block, as the
+// blocks of k_adjoint).
+template <class St, bool MRT, bool SOFT>
+__device__ __forceinline__ void adjoint_pair_interior_part(const AdjPairArgs<St>& P, int iblock) {
+  double gr = adjoint_pair_interior<St, MRT, SOFT>(P, iblock);
+  if (SOFT && (P.A.s.flags & SF_SOLID_SPHERE)) {
+#pragma unroll
+    for (int o = 16; o > 0; o >>= 1) gr += __shfl_down_sync(0xffffffffu, gr, o);
+    if ((threadIdx.x & 31) == 0)
+      P.A.gr_partials[size_t(iblock) * 8 + (threadIdx.x >> 5)] += gr;
+  }
+}
+
+template <class St, bool MRT, bool SOFT>
+__global__ void __launch_bounds__(kAdjPairBlock, LBM_ADJ_PAIR_MINB)
+    k_adjoint_pair(const AdjPairArgs<St> P, int nlist) {
+  if (int(blockIdx.x) < nlist)
+    adjoint_pair_list_part<St, MRT>(P, blockIdx.x);
+  else
+    adjoint_pair_interior_part<St, MRT, SOFT>(P, blockIdx.x - nlist);
 }
 
 // nu_N = Z^T lambda_N with lambda_N = dJ/df_N from the momentum exchange:
@@ -569,13 +624,12 @@ static inline int nblk(int n) { return (n + 255) / 256; }
 template <class St>
 cudaError_t launch_adjoint(const AdjArgs<typename Storage<St>::Re>& A, bool mrt,
                            cudaStream_t st) {
-  // FP32 arithmetic (FP32 / FP16 / BF16 storage), nz even, no porosity blend:
-  // k_adjoint_pair, one launch of list blocks + interior blocks (176 / 178 us
-  // per 256x128x128 step against 280 / 265 us for k_adjoint)
+  // FP32 arithmetic (FP32 / FP16 / BF16 storage), nz even: k_adjoint_pair,
+  // one launch of list blocks + interior blocks (166 us per 256x128x128 step
+  // against 280 / 265 us for k_adjoint); SOFT for a porosity blend
   if constexpr (sizeof(typename Storage<St>::Re) == 4) {
     const Grid& g = A.s.g;
-    if ((g.nz % 2) == 0 && A.s.spec_adj &&
-        !(A.s.flags & (SF_SOLID_SPHERE | SF_SOLID_FIELD))) {
+    if ((g.nz % 2) == 0 && A.s.spec_adj) {
       AdjPairArgs<St> P;
       P.A = A;
       const long long N = g.n, nyz = (long long)g.ny * g.nz;
@@ -589,10 +643,15 @@ cudaError_t launch_adjoint(const AdjArgs<typename Storage<St>::Re>& A, bool mrt,
       }
       const int nb = (g.n / 2 + kAdjPairBlock - 1) / kAdjPairBlock;
       const int nlist = (2 * A.s.spec_adj_count + kAdjPairBlock - 1) / kAdjPairBlock;
-      if (mrt)
-        k_adjoint_pair<St, true><<<nlist + nb, kAdjPairBlock, 0, st>>>(P, nlist);
+      const bool soft = (A.s.flags & (SF_SOLID_SPHERE | SF_SOLID_FIELD)) != 0;
+      if (mrt && soft)
+        k_adjoint_pair<St, true, true><<<nlist + nb, kAdjPairBlock, 0, st>>>(P, nlist);
+      else if (mrt)
+        k_adjoint_pair<St, true, false><<<nlist + nb, kAdjPairBlock, 0, st>>>(P, nlist);
+      else if (soft)
+        k_adjoint_pair<St, false, true><<<nlist + nb, kAdjPairBlock, 0, st>>>(P, nlist);
       else
-        k_adjoint_pair<St, false><<<nlist + nb, kAdjPairBlock, 0, st>>>(P, nlist);
+        k_adjoint_pair<St, false, false><<<nlist + nb, kAdjPairBlock, 0, st>>>(P, nlist);
       return cudaGetLastError();
     }
   }
@@ -659,6 +718,58 @@ __global__ void __launch_bounds__(256, LBM_ADJ_BATCH_MINB)
   for (int sb = m.y; sb < end; ++sb) adjoint_body<St, MRT>(A, sb);
 }
 
+// Batched k_adjoint_pair (FP32 storage, nz even): map[b] = (instance, first
+// sub-block), the sub-blocks of an instance being its list blocks then its
+// interior blocks, kBatchChunk per block; entries with instance -1 pad the
+// map to the grid the launch (and a captured graph) was sized for.  SOFT:
+// the instances with a porosity blend.
+template <bool MRT, bool SOFT>
+__global__ void __launch_bounds__(kAdjPairBlock, LBM_ADJ_PAIR_MINB)
+    k_adjoint_pair_batch(const AdjArgs<float>* __restrict__ args,
+                         const BatchInst* __restrict__ inst, const int2* __restrict__ map,
+                         int sprev_slot, int sk_slot, int nu_in_slot, int nu_out_slot, int first,
+                         int last) {
+  __shared__ AdjPairArgs<float> P;
+  const int2 m = map[blockIdx.x];
+  if (m.x < 0) return;
+  copy_to_shared(&P.A, args + m.x);
+  __syncthreads();
+  const BatchInst& b = inst[m.x];
+  if (threadIdx.x == 0) {
+    AdjArgs<float>& A = P.A;
+    A.s.src = batch_slot(b, sprev_slot);
+    A.S_k = batch_slot(b, sk_slot);
+    A.nu_in = static_cast<const float*>(batch_slot(b, nu_in_slot));
+    A.nu_out = static_cast<float*>(batch_slot(b, nu_out_slot));
+    A.first = first;
+    A.last = last;
+    A.dj_dfx = b.out + 4;
+    A.gr_partials = b.gr_part;
+    A.gq = b.gq;
+    const Grid& g = A.s.g;
+    const long long N = g.n, nyz = (long long)g.ny * g.nz;
+#pragma unroll
+    for (int i = 0; i < Q; ++i) {
+      const long long off = ex(i) * nyz + ey(i) * g.nz + ez(i);
+      P.pull[i] = static_cast<const float*>(A.s.src) + i * N - off;
+      P.push[i] = A.nu_in + i * N + off;
+      P.out[i] = A.nu_out + i * N;
+      P.soff2[0][i] = make_float2(0.0f, 0.0f);
+      P.soff2[1][i] = make_float2(0.0f, 0.0f);
+    }
+  }
+  __syncthreads();
+  const int nlist = (2 * P.A.s.spec_adj_count + kAdjPairBlock - 1) / kAdjPairBlock;
+  const int nint = (P.A.s.g.n / 2 + kAdjPairBlock - 1) / kAdjPairBlock;
+  const int end = m.y + kBatchChunk < nlist + nint ? m.y + kBatchChunk : nlist + nint;
+  for (int sb = m.y; sb < end; ++sb) {
+    if (sb < nlist)
+      adjoint_pair_list_part<float, MRT>(P, sb);
+    else
+      adjoint_pair_interior_part<float, MRT, SOFT>(P, sb - nlist);
+  }
+}
+
 __global__ void __launch_bounds__(256)
     k_adjoint_seed_batch(const StepArgs<float>* __restrict__ args,
                          const BatchInst* __restrict__ inst, const int2* __restrict__ map,
@@ -677,7 +788,7 @@ __global__ void __launch_bounds__(256)
 // Per instance (one block each): clear the dJ/dr partials and the per-link dJ/dq.
 __global__ void __launch_bounds__(256) k_zero_grad_batch(const BatchInst* __restrict__ inst) {
   const BatchInst& b = inst[blockIdx.x];
-  for (int i = threadIdx.x; i < b.nblk * 8; i += blockDim.x) b.gr_part[i] = 0.0;
+  for (int i = threadIdx.x; i < b.ngr; i += blockDim.x) b.gr_part[i] = 0.0;
   for (int i = threadIdx.x; i < b.ngq; i += blockDim.x) b.gq[i] = 0.0;
 }
 
@@ -686,7 +797,7 @@ __global__ void __launch_bounds__(256) k_reduce_gr_batch(const BatchInst* __rest
   __shared__ double sh[256];
   const BatchInst& b = inst[blockIdx.x];
   double v = 0.0;
-  for (int i = threadIdx.x; i < b.nblk * 8; i += blockDim.x) v += b.gr_part[i];
+  for (int i = threadIdx.x; i < b.ngr; i += blockDim.x) v += b.gr_part[i];
   sh[threadIdx.x] = v;
   __syncthreads();
   for (int o = blockDim.x / 2; o > 0; o >>= 1) {
@@ -735,6 +846,25 @@ cudaError_t launch_adjoint_batch(const AdjArgs<float>* args, const BatchInst* in
   else
     k_adjoint_batch<St, false><<<nblocks, block, 0, st>>>(args, inst, map, sprev_slot, sk_slot,
                                                          nu_in_slot, nu_out_slot, first, last);
+  return cudaGetLastError();
+}
+
+cudaError_t launch_adjoint_pair_batch(const AdjArgs<float>* args, const BatchInst* inst,
+                                      const int2* map, int nblocks, bool mrt, bool soft,
+                                      int sprev_slot, int sk_slot, int nu_in_slot,
+                                      int nu_out_slot, int first, int last, cudaStream_t st) {
+  if (mrt && soft)
+    k_adjoint_pair_batch<true, true><<<nblocks, kAdjPairBlock, 0, st>>>(
+        args, inst, map, sprev_slot, sk_slot, nu_in_slot, nu_out_slot, first, last);
+  else if (mrt)
+    k_adjoint_pair_batch<true, false><<<nblocks, kAdjPairBlock, 0, st>>>(
+        args, inst, map, sprev_slot, sk_slot, nu_in_slot, nu_out_slot, first, last);
+  else if (soft)
+    k_adjoint_pair_batch<false, true><<<nblocks, kAdjPairBlock, 0, st>>>(
+        args, inst, map, sprev_slot, sk_slot, nu_in_slot, nu_out_slot, first, last);
+  else
+    k_adjoint_pair_batch<false, false><<<nblocks, kAdjPairBlock, 0, st>>>(
+        args, inst, map, sprev_slot, sk_slot, nu_in_slot, nu_out_slot, first, last);
   return cudaGetLastError();
 }
 

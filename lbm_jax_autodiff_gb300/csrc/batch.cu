@@ -34,6 +34,10 @@ cudaError_t launch_adjoint_batch(const AdjArgs<float>* args, const BatchInst* in
                                  const int2* map, int nblocks, int block, bool mrt,
                                  int sprev_slot, int sk_slot, int nu_in_slot, int nu_out_slot,
                                  int first, int last, cudaStream_t st);
+cudaError_t launch_adjoint_pair_batch(const AdjArgs<float>* args, const BatchInst* inst,
+                                      const int2* map, int nblocks, bool mrt, bool soft,
+                                      int sprev_slot, int sk_slot, int nu_in_slot,
+                                      int nu_out_slot, int first, int last, cudaStream_t st);
 cudaError_t launch_adjoint_seed_batch(const StepArgs<float>* args, const BatchInst* inst,
                                       const int2* map, int nblocks, int block, int nu_slot,
                                       cudaStream_t st);
@@ -45,6 +49,13 @@ cudaError_t launch_adam_batch(const BatchInst* inst, int count, const AdamP& p, 
 namespace {
 
 constexpr int kMinBlock = 128;   // partial buffers are sized for the smallest block
+constexpr int kPairBlock = 128;  // threads (pairs) per block of k_adjoint_pair_batch
+
+// dJ/dr partial slots of an instance of n cells: 8 per block of the smallest
+// block size covers both k_adjoint_batch (8 per block) and
+// k_adjoint_pair_batch (8 per 256-cell interior block, then one per list
+// warp, at most n / 32 of them), plus slack for the rounding of both.
+size_t gr_slots(size_t n) { return (n + kMinBlock - 1) / kMinBlock * 8 + 64; }
 
 // f_i = value[i] on every cell
 __global__ void k_fill_dirs(float* __restrict__ f, int n, Consts<float> v) {
@@ -67,6 +78,12 @@ struct lbm_batch {
   // device tables
   int nmap = 0;
   int2* d_map = nullptr;
+  // block maps of k_adjoint_pair_batch: [0] instances without, [1] with a
+  // porosity blend; pmap_cap entries each (the launch grid), padded with -1
+  bool pair_adjoint = false;
+  int2* d_pmap[2] = {nullptr, nullptr};
+  int pmap_cap[2] = {0, 0};
+  int pmap_used[2] = {0, 0};
   BatchInst* d_inst = nullptr;
   StepArgs<float>* d_sargs = nullptr;
   AdjArgs<float>* d_aargs = nullptr;
@@ -119,6 +136,50 @@ int build_map(lbm_batch* b) {
   return LBM_OK;
 }
 
+void drop_graph(lbm_batch* b);
+
+// Block maps of the pair adjoint from the instances' current adjoint lists:
+// per instance its list blocks then its interior blocks, kBatchChunk per map
+// entry, largest instances first.  A map only grows (padded with -1 entries)
+// so the grid of a captured graph stays valid; growth drops the graph.
+int build_pmaps(lbm_batch* b) {
+  b->pair_adjoint = true;
+  for (auto* s : b->sims)
+    if ((s->g.nz % 2) != 0 || !s->spec_adj) b->pair_adjoint = false;
+  if (!b->pair_adjoint) return LBM_OK;
+  std::vector<int> order(b->count);
+  for (int i = 0; i < b->count; ++i) order[i] = i;
+  std::stable_sort(order.begin(), order.end(),
+                   [&](int x, int y) { return b->sims[x]->n > b->sims[y]->n; });
+  std::vector<int2> map[2];
+  for (int i : order) {
+    const lbm_sim* s = b->sims[i];
+    const int soft = (s->porosity_mode == LBM_POROSITY_SOFT) ? 1 : 0;
+    const int nlist = (2 * s->nspec_adj + kPairBlock - 1) / kPairBlock;
+    const int nint = int((s->n / 2 + kPairBlock - 1) / kPairBlock);
+    for (int j = 0; j < nlist + nint; j += kBatchChunk) map[soft].push_back(make_int2(i, j));
+  }
+  for (int m = 0; m < 2; ++m) {
+    const int need = int(map[m].size());
+    if (need > b->pmap_cap[m]) {
+      drop_graph(b);
+      cudaFree(b->d_pmap[m]);
+      b->d_pmap[m] = nullptr;
+      b->pmap_cap[m] = 0;
+      const int cap = need + need / 8 + 64;
+      LBM_TRY(dev_alloc((void**)&b->d_pmap[m], size_t(cap) * sizeof(int2)));
+      b->pmap_cap[m] = cap;
+    }
+    b->pmap_used[m] = need;
+    if (b->pmap_cap[m] == 0) continue;
+    map[m].resize(b->pmap_cap[m], make_int2(-1, 0));
+    LBM_TRY(cuda_check(cudaMemcpy(b->d_pmap[m], map[m].data(), map[m].size() * sizeof(int2),
+                                  cudaMemcpyHostToDevice),
+                       "pair map H2D"));
+  }
+  return LBM_OK;
+}
+
 // Rewrite the per-instance argument tables from the handles (after geometry,
 // workspace or block-size changes).  Synchronous: the tables are read by
 // kernels (also by replays of a captured graph) only after this returns.
@@ -145,6 +206,7 @@ int refresh_tables(lbm_batch* b) {
     t.state_bytes = s->n * Q * s->st_bytes;
     t.force_part = b->force_part[i];
     t.gr_part = b->gr_part[i];
+    t.ngr = int(gr_slots(s->n));
     t.gq = s->gq;
     t.ngq = s->gq ? s->nrec * Q : 0;
     t.nblk = int((s->n + b->block - 1) / b->block);
@@ -160,7 +222,7 @@ int refresh_tables(lbm_batch* b) {
                                 cudaMemcpyHostToDevice), "inst H2D"));
   LBM_TRY(cuda_check(cudaMemcpy(b->d_dyn, dyn.data(), dyn.size() * sizeof(double),
                                 cudaMemcpyHostToDevice), "area H2D"));
-  return LBM_OK;
+  return build_pmaps(b);
 }
 
 int require_geometry(const lbm_batch* b, const char* who) {
@@ -282,11 +344,22 @@ int enqueue_grad(lbm_batch* b, int N, int K, const AdamP* adam, cudaStream_t st)
     for (int k = b0 - 1; k >= a0; --k) {
       const int sprev = (k == a0) ? slot0 : stash(k - a0);
       const int nin = cur ? SLOT_NU1 : SLOT_NU0, nout = cur ? SLOT_NU0 : SLOT_NU1;
-      LBM_TRY(cuda_check(launch_adjoint_batch<float>(b->d_aargs, b->d_inst, b->d_map, b->nmap,
-                                                     b->block, b->mrt, sprev,
-                                                     stash(k - a0 + 1), nin, nout, k == 0,
-                                                     k == N - 1, st),
-                         "k_adjoint_batch launch"));
+      if (b->pair_adjoint) {
+        // instances without and with a porosity blend, one launch each
+        for (int m = 0; m < 2; ++m)
+          if (b->pmap_used[m] > 0)
+            LBM_TRY(cuda_check(
+                launch_adjoint_pair_batch(b->d_aargs, b->d_inst, b->d_pmap[m], b->pmap_cap[m],
+                                          b->mrt, m == 1, sprev, stash(k - a0 + 1), nin, nout,
+                                          k == 0, k == N - 1, st),
+                "k_adjoint_pair_batch launch"));
+      } else {
+        LBM_TRY(cuda_check(launch_adjoint_batch<float>(b->d_aargs, b->d_inst, b->d_map, b->nmap,
+                                                       b->block, b->mrt, sprev,
+                                                       stash(k - a0 + 1), nin, nout, k == 0,
+                                                       k == N - 1, st),
+                           "k_adjoint_batch launch"));
+      }
       cur = 1 - cur;
     }
   }
@@ -383,7 +456,7 @@ int lbm_batch_create(const lbm_params* params, int count, lbm_batch** out) {
       double *fp = nullptr, *gp = nullptr;
       if ((rc = dev_alloc((void**)&fp, nb * 3 * sizeof(double)))) break;
       b->force_part.push_back(fp);
-      if ((rc = dev_alloc((void**)&gp, nb * 8 * sizeof(double)))) break;
+      if ((rc = dev_alloc((void**)&gp, gr_slots(b->sims[i]->n) * sizeof(double)))) break;
       b->gr_part.push_back(gp);
     }
     if (rc) break;
@@ -415,6 +488,8 @@ int lbm_batch_destroy(lbm_batch* b) {
   for (auto* p : b->force_part) cudaFree(p);
   for (auto* p : b->gr_part) cudaFree(p);
   cudaFree(b->d_map);
+  cudaFree(b->d_pmap[0]);
+  cudaFree(b->d_pmap[1]);
   cudaFree(b->d_inst);
   cudaFree(b->d_sargs);
   cudaFree(b->d_aargs);

@@ -28,7 +28,8 @@ struct BatchInst {
   char* states;
   unsigned long long state_bytes;
   double* force_part;      // [nblk][3]
-  double* gr_part;         // [nblk][8]
+  double* gr_part;         // [ngr] dJ/dr partials: per-block slots, then per-warp list slots
+  int ngr;
   double* gq;              // [ngq] per-link dJ/dq
   int ngq;
   int nblk;                // blocks of this instance at the batch block size

@@ -204,3 +204,54 @@ def test_fp16_paths_vs_fp32(cuda, nx, ny, nz, periodic):
     cd16, g16 = run("fp16")
     assert abs(cd16 - cd32) <= 1e-3 * abs(cd32), (cd16, cd32)
     assert abs(g16 - g32) <= 1e-3 * abs(g32), (g16, g32)
+
+
+@pytest.mark.parametrize("collision,smag,q_mode,periodic", [
+    ("mrt", 0.1, "bouzidi", True),
+    ("bgk", None, "halfway", False),     # non-periodic edges in the list
+    ("mrt", None, "halfway", True),
+])
+def test_fp32_soft_sphere_vs_fp64(cuda, collision, smag, q_mode, periodic):
+    """Sigmoid-porosity sphere: the FP32 packed adjoint (porosity-blend
+    transpose and dJ/dp on the pairs) within 1e-3 of the FP64 per-cell one."""
+    nx, ny, nz, n, tau = 32, 16, 16, 60, 0.56
+
+    def run(st):
+        sim = _sim(nx, ny, nz, tau, collision=collision, storage=st,
+                   use_smagorinsky=smag is not None, smagorinsky_cs=smag or 0.1,
+                   periodic_yz=periodic)
+        sim.set_sphere(0.5, kind="sigmoid", q_mode=q_mode, porosity="soft", sharpness=20.0)
+        sim.set_state(sim.equilibrium_state())
+        out = sim.cd_and_grad(n, checkpoint_every=20)
+        sim.close()
+        return out
+
+    cd64, g64 = run("fp64")
+    cd32, g32 = run("fp32")
+    assert abs(cd32 - cd64) <= 2e-4 * abs(cd64), (cd32, cd64)
+    assert abs(g32 - g64) <= 1e-3 * abs(g64), (g32, g64)
+
+
+def test_fp32_porosity_field_vs_fp64(cuda):
+    """Porosity given as a field (mask geometry): dCd/dq of the FP32 packed
+    adjoint within 1e-3 of the FP64 per-cell one."""
+    from oracle import geometry
+    nx, ny, nz, n, tau = 32, 16, 16, 60, 0.56
+
+    def run(st, dt):
+        por, solid, q = geometry.sphere_geometry(nx, ny, nz, 0.5, "bouzidi", "soft", 20.0)
+        sim = _sim(nx, ny, nz, tau, storage=st)
+        sim.set_mask(solid.to(torch.int32).cuda(), q.to(dt).cuda().contiguous(),
+                     porosity=por.to(dt).cuda().contiguous())
+        sim.set_state(sim.equilibrium_state())
+        cd, _, ex = sim.cd_and_grad(n, checkpoint_every=20, dcd_dq=True)
+        gq = ex["dcd_dq"].double().cpu()
+        sim.close()
+        return cd, gq
+
+    cd64, gq64 = run("fp64", torch.float64)
+    cd32, gq32 = run("fp32", torch.float32)
+    assert abs(cd32 - cd64) <= 2e-4 * abs(cd64), (cd32, cd64)
+    scale = gq64.abs().max().item()
+    assert scale > 0.0
+    assert (gq32 - gq64).abs().max().item() <= 1e-3 * scale
