@@ -300,10 +300,10 @@ def _batch_rate(n_steps, barrier, max_over_ranks):
     h1 = b.optimize(1, n_steps, **kw)            # graph replay
     t = max_over_ranks(time.perf_counter() - t0)
     blk, seg, rec, wbytes, graph_s = b.plan
+    launches = b.graph_launches
     cells = b.cells
     b.close()
     torch.cuda.empty_cache()
-    launches = 2 * n_steps + rec + 6   # fwd, stream+force, finalize, zero, seed, recompute, adjoint, reduce, adam
     return {"instances": len(inst), "cells": cells, "block": blk, "segment_steps": seg,
             "recomputed_steps": rec, "workspace_gb": round(wbytes / 1e9, 1),
             "autotune_s": round(t_tune, 2), "graph_capture_s": round(graph_s, 3),

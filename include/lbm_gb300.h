@@ -373,6 +373,9 @@ int lbm_batch_autotune(lbm_batch* batch, int probe_steps, int n_steps, int* bloc
                        int* checkpoint_out, void* stream);
 int lbm_batch_get_plan(lbm_batch* batch, int* block, int* segment_steps, int* recomputed_steps,
                        unsigned long long* workspace_bytes, double* graph_build_seconds);
+/* Kernel launches (graph nodes) of the last captured gradient evaluation
+ * (0 before the first capture). */
+int lbm_batch_graph_launches(lbm_batch* batch, long long* launches);
 
 #ifdef __cplusplus
 }

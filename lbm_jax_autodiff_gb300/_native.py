@@ -165,6 +165,7 @@ SIGNATURES = {
     "lbm_batch_autotune": [_vp, _i, _i, ctypes.POINTER(_i), ctypes.POINTER(_i), _vp],
     "lbm_batch_get_plan": [_vp, ctypes.POINTER(_i), ctypes.POINTER(_i), ctypes.POINTER(_i),
                            ctypes.POINTER(ctypes.c_ulonglong), ctypes.POINTER(_d)],
+    "lbm_batch_graph_launches": [_vp, ctypes.POINTER(ctypes.c_longlong)],
 }
 _RESTYPES = {"lbm_status_string": ctypes.c_char_p, "lbm_last_error": ctypes.c_char_p}
 

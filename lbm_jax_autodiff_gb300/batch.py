@@ -159,6 +159,13 @@ class Batch:
                  ctypes.byref(r), ctypes.byref(w), ctypes.byref(g))
         return b.value, k.value, r.value, w.value, g.value
 
+    @property
+    def graph_launches(self):
+        """Kernel launches in the last captured gradient-evaluation graph."""
+        n = ctypes.c_longlong()
+        nat.call("lbm_batch_graph_launches", self._h, ctypes.byref(n))
+        return n.value
+
 
 def config5_instances(count=64, seed=0, n_alpha=(5.0, 10.0, 20.0), re=50.0):
     """The batched workload: grids uniform over {64x32x32, 96x48x48,

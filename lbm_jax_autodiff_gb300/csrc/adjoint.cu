@@ -723,8 +723,12 @@ __global__ void __launch_bounds__(256, LBM_ADJ_BATCH_MINB)
 // interior blocks, kBatchChunk per block; entries with instance -1 pad the
 // map to the grid the launch (and a captured graph) was sized for.  SOFT:
 // the instances with a porosity blend.
+#ifndef LBM_ADJ_PAIR_BATCH_MINB
+#define LBM_ADJ_PAIR_BATCH_MINB 4
+#endif
+
 template <bool MRT, bool SOFT>
-__global__ void __launch_bounds__(kAdjPairBlock, LBM_ADJ_PAIR_MINB)
+__global__ void __launch_bounds__(kAdjPairBlock, LBM_ADJ_PAIR_BATCH_MINB)
     k_adjoint_pair_batch(const AdjArgs<float>* __restrict__ args,
                          const BatchInst* __restrict__ inst, const int2* __restrict__ map,
                          int sprev_slot, int sk_slot, int nu_in_slot, int nu_out_slot, int first,

@@ -105,6 +105,7 @@ struct lbm_batch {
   int g_N = -1, g_K = -1, g_block = -1, g_adam = -1;
   AdamP g_p{};
   double graph_seconds = 0.0;
+  long long graph_launches = 0;   // kernel nodes of the captured graph
 };
 
 namespace {
@@ -395,6 +396,13 @@ int run_grad(lbm_batch* b, int N, int K, const AdamP* adam, int use_graph, cudaS
       return rc;
     }
     LBM_TRY(cuda_check(ec, "end capture"));
+    size_t nodes = 0;
+    const cudaError_t en = cudaGraphGetNodes(graph, nullptr, &nodes);
+    if (en != cudaSuccess) {
+      cudaGraphDestroy(graph);
+      return cuda_check(en, "graph nodes");
+    }
+    b->graph_launches = (long long)nodes;
     const cudaError_t ei = cudaGraphInstantiate(&b->gexec, graph, 0);
     cudaGraphDestroy(graph);
     LBM_TRY(cuda_check(ei, "graph instantiate"));
@@ -751,6 +759,12 @@ int lbm_batch_get_plan(lbm_batch* b, int* block, int* segment_steps, int* recomp
   *recomputed_steps = b->plan_recompute;
   *workspace_bytes = b->plan_bytes;
   *graph_build_seconds = b->graph_seconds;
+  return LBM_OK;
+}
+
+int lbm_batch_graph_launches(lbm_batch* b, long long* launches) {
+  if (!b || !launches) return set_error(LBM_ERR_ARG, "lbm_batch_graph_launches: null argument");
+  *launches = b->graph_launches;
   return LBM_OK;
 }
 
