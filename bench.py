@@ -359,10 +359,8 @@ def run_ours(args):
     f_out = torch.empty_like(f_host).pin_memory()
     cd_host = torch.empty((1, 4), dtype=torch.float64).pin_memory()
     f_dev = torch.empty_like(f_host, device="cuda")
-    barrier()
-    torch.cuda.synchronize()
-    t0 = time.perf_counter()
-    for _ in range(n_chunks):
+
+    def e2e_chunk():
         f_dev.copy_(f_host, non_blocking=True)
         sim.set_state(f_dev)
         s = sim.run(chunk, sample_every=chunk)
@@ -370,6 +368,15 @@ def run_ours(args):
         f_out.copy_(f_dev, non_blocking=True)
         cd_host.copy_(s, non_blocking=True)
         torch.cuda.synchronize()
+
+    # one untimed chunk: the first device access to freshly pinned host pages
+    # costs ~250 ms once (measured 310 ms for the first chunk, 61 ms after)
+    e2e_chunk()
+    barrier()
+    torch.cuda.synchronize()
+    t0 = time.perf_counter()
+    for _ in range(n_chunks):
+        e2e_chunk()
     t_e2e = max_over_ranks(time.perf_counter() - t0)
     e2e_mlups = ws * n_cells * chunk * n_chunks / t_e2e / 1e6
     state_bytes = 19 * n_cells * 4
@@ -438,8 +445,8 @@ def run_ours(args):
             "e2e": {"value": round(e2e_mlups, 1), "unit": "MLUPS",
                     "h2d_bytes_per_step": state_bytes // chunk,
                     "d2h_bytes_per_step": (state_bytes + 32) // chunk,
-                    "note": "public API, host pinned state in/out every %d-step chunk, Cd read back"
-                            % chunk},
+                    "note": "public API, host pinned state in/out every %d-step chunk, Cd read "
+                            "back; one untimed warm-up chunk" % chunk},
             "gpu_launches": args.steps,
             "clocks": clk,
             "storage16": extra,
