@@ -485,9 +485,9 @@ __device__ __forceinline__ double adjoint_pair_interior(const AdjPairArgs<St>& P
     for (int j = 0; j < Q; ++j) {
       const int b = ey(j) == 1 ? iyp : (ey(j) == -1 ? iym : idx);
       const float* p = P.push[j] + b;
-      if (ez(j) == 0) mu[j] = V2(__ldg(reinterpret_cast<const float2*>(p)));
-      else if (ez(j) == 1) mu[j] = V2(__ldg(p), __ldg(p + 1 + zw1));
-      else mu[j] = V2(__ldg(p + zw0), __ldg(p + 1));
+      if (ez(j) == 0) mu[j] = V2(ldg_s(reinterpret_cast<const float2*>(p)));
+      else if (ez(j) == 1) mu[j] = V2(ldg_s(p), ldg_s(p + 1 + zw1));
+      else mu[j] = V2(ldg_s(p + zw0), ldg_s(p + 1));
     }
   }
   // f_k

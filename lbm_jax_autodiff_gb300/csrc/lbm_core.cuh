@@ -13,6 +13,7 @@
 #pragma once
 
 #include <cmath>
+#include <cstring>
 #include <cstdint>
 #include <cuda_bf16.h>
 #include <cuda_fp16.h>
@@ -84,10 +85,70 @@ __host__ __device__ constexpr bool is_conserved(int k) {
 // f_i - w from a per-direction offset w that the caller passes (the solver
 // uses the free-stream equilibrium); arithmetic stays FP32.
 // ---------------------------------------------------------------------------
+// Read-only global loads of the population sweeps with a 256-byte L2
+// prefetch (ld.global.nc.L2::256B): the sweeps stream through HBM, and
+// fetching the whole 256-byte span an access falls in measured about 1 %
+// faster per FP32 step than plain ld.global.nc.
+#ifndef LBM_L2_PREFETCH
+#define LBM_L2_PREFETCH 1
+#endif
+__device__ __forceinline__ float ldg_s(const float* p) {
+#if LBM_L2_PREFETCH
+  float v;
+  asm("ld.global.nc.L2::256B.f32 %0, [%1];" : "=f"(v) : "l"(p));
+  return v;
+#else
+  return __ldg(p);
+#endif
+}
+__device__ __forceinline__ float2 ldg_s(const float2* p) {
+#if LBM_L2_PREFETCH
+  float2 v;
+  asm("ld.global.nc.L2::256B.v2.f32 {%0, %1}, [%2];" : "=f"(v.x), "=f"(v.y) : "l"(p));
+  return v;
+#else
+  return __ldg(p);
+#endif
+}
+__device__ __forceinline__ unsigned short ldg_s16(const void* p) {
+#if LBM_L2_PREFETCH
+  unsigned short v;
+  asm("ld.global.nc.L2::256B.b16 %0, [%1];" : "=h"(v) : "l"(p));
+  return v;
+#else
+  return __ldg(static_cast<const unsigned short*>(p));
+#endif
+}
+__device__ __forceinline__ unsigned ldg_s32(const void* p) {
+#if LBM_L2_PREFETCH
+  unsigned v;
+  asm("ld.global.nc.L2::256B.b32 %0, [%1];" : "=r"(v) : "l"(p));
+  return v;
+#else
+  return __ldg(static_cast<const unsigned*>(p));
+#endif
+}
+__device__ __forceinline__ __half ldg_s(const __half* p) { return __ushort_as_half(ldg_s16(p)); }
+__device__ __forceinline__ __nv_bfloat16 ldg_s(const __nv_bfloat16* p) {
+  return __ushort_as_bfloat16(ldg_s16(p));
+}
+__device__ __forceinline__ __half2 ldg_s(const __half2* p) {
+  const unsigned u = ldg_s32(p);
+  __half2 h;
+  memcpy(&h, &u, 4);
+  return h;
+}
+__device__ __forceinline__ __nv_bfloat162 ldg_s(const __nv_bfloat162* p) {
+  const unsigned u = ldg_s32(p);
+  __nv_bfloat162 h;
+  memcpy(&h, &u, 4);
+  return h;
+}
+
 template <class St> struct Storage;
 template <> struct Storage<float> {
   using Re = float;
-  static __device__ __forceinline__ float ld(const float* p, float) { return __ldg(p); }
+  static __device__ __forceinline__ float ld(const float* p, float) { return ldg_s(p); }
   static __device__ __forceinline__ void st(float* p, float v, float) { *p = v; }
 };
 template <> struct Storage<double> {
@@ -98,7 +159,7 @@ template <> struct Storage<double> {
 template <> struct Storage<__half> {
   using Re = float;
   static __device__ __forceinline__ float ld(const __half* p, float w) {
-    return w + __half2float(__ldg(p));
+    return w + __half2float(ldg_s(p));
   }
   static __device__ __forceinline__ void st(__half* p, float v, float w) {
     *p = __float2half_rn(v - w);
@@ -107,7 +168,7 @@ template <> struct Storage<__half> {
 template <> struct Storage<__nv_bfloat16> {
   using Re = float;
   static __device__ __forceinline__ float ld(const __nv_bfloat16* p, float w) {
-    return w + __bfloat162float(__ldg(p));
+    return w + __bfloat162float(ldg_s(p));
   }
   static __device__ __forceinline__ void st(__nv_bfloat16* p, float v, float w) {
     *p = __float2bfloat16_rn(v - w);

@@ -82,10 +82,10 @@ template <> struct ScalarOf<V2> { using type = float; };
 template <class St> struct Pair;
 template <> struct Pair<float> {
   static __device__ __forceinline__ V2 ld2(const float* p, V2) {
-    return V2(__ldg(reinterpret_cast<const float2*>(p)));
+    return V2(ldg_s(reinterpret_cast<const float2*>(p)));
   }
   static __device__ __forceinline__ V2 ld2s(const float* p0, const float* p1, V2) {
-    return V2(__ldg(p0), __ldg(p1));
+    return V2(ldg_s(p0), ldg_s(p1));
   }
   static __device__ __forceinline__ void st2(float* p, V2 v, V2) {
     *reinterpret_cast<float2*>(p) = v.v;
@@ -103,10 +103,10 @@ __device__ __forceinline__ float add_bf16(__nv_bfloat16 h, float c) {
 
 template <> struct Pair<__half> {
   static __device__ __forceinline__ V2 ld2(const __half* p, V2 w) {
-    return V2(__half22float2(__ldg(reinterpret_cast<const __half2*>(p)))) + w;
+    return V2(__half22float2(ldg_s(reinterpret_cast<const __half2*>(p)))) + w;
   }
   static __device__ __forceinline__ V2 ld2s(const __half* p0, const __half* p1, V2 w) {
-    return V2(__half22float2(__halves2half2(__ldg(p0), __ldg(p1)))) + w;
+    return V2(__half22float2(__halves2half2(ldg_s(p0), ldg_s(p1)))) + w;
   }
   static __device__ __forceinline__ void st2(__half* p, V2 v, V2 w) {
     *reinterpret_cast<__half2*>(p) = __float22half2_rn((v - w).v);
@@ -114,12 +114,12 @@ template <> struct Pair<__half> {
 };
 template <> struct Pair<__nv_bfloat16> {
   static __device__ __forceinline__ V2 ld2(const __nv_bfloat16* p, V2 w) {
-    const __nv_bfloat162 v = __ldg(reinterpret_cast<const __nv_bfloat162*>(p));
+    const __nv_bfloat162 v = ldg_s(reinterpret_cast<const __nv_bfloat162*>(p));
     return V2(add_bf16(__low2bfloat16(v), w.x()), add_bf16(__high2bfloat16(v), w.y()));
   }
   static __device__ __forceinline__ V2 ld2s(const __nv_bfloat16* p0, const __nv_bfloat16* p1,
                                             V2 w) {
-    return V2(add_bf16(__ldg(p0), w.x()), add_bf16(__ldg(p1), w.y()));
+    return V2(add_bf16(ldg_s(p0), w.x()), add_bf16(ldg_s(p1), w.y()));
   }
   static __device__ __forceinline__ void st2(__nv_bfloat16* p, V2 v, V2 w) {
     *reinterpret_cast<__nv_bfloat162*>(p) = __float22bfloat162_rn((v - w).v);
