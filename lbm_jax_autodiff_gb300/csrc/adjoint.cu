@@ -352,10 +352,10 @@ constexpr int kAdjPairBlock = 128;   // 256 cells per block, as k_adjoint
 #define LBM_ADJ_PAIR_MINB 4
 #endif
 
-// The part of a pair's adjoint step after mu and f_k: the transpose B^T of
-// the hard bounce-back or (SOFT) of the porosity blend, with dJ/dp for a
-// sigmoid sphere; lambda_k = C^T mu on the packed values; Zou-He transposes
-// on the faces; store of nu_k.  Returns the pair's dJ/dr contribution
+// The part of an interior pair's adjoint step after mu and f_k: the
+// transpose B^T of the hard bounce-back or (SOFT) of the porosity blend, with
+// dJ/dp for a sigmoid sphere; lambda_k = C^T mu on the packed values; store
+// of nu_k.  Returns the pair's dJ/dr contribution
 // (nonzero only for a sigmoid sphere).
 template <class St, bool MRT, bool SOFT>
 __device__ __forceinline__ double adj_pair_finish(const AdjPairArgs<St>& P, int idx, int x, int y,
@@ -412,20 +412,7 @@ __device__ __forceinline__ double adj_pair_finish(const AdjPairArgs<St>& P, int 
   cell_scalars<V2>(f, cs);
   collide_vjp_s<V2>(cs, f, mu, V2(a.tau), MRT, (fl & SF_SMAG) != 0, V2(a.c18cs2), K,
                     static_cast<V2*>(nullptr));
-  // nu_k = Z^T lambda_k on the faces (both cells of a pair share x)
-  if (!A.first) {
-    if (x == g.nx - 1 && !(fl & SF_NO_OUTLET)) zou_he_outlet_T<V2>(mu, V2(a.rho_out));
-    if (x == 0 && !(fl & SF_NO_INLET)) {
-      V2 ux(a.u_in[0]), uy(a.u_in[1]), uz(a.u_in[2]);
-      if (fl & SF_INLET_FACE) {
-        const int fi = y * g.nz + z, fn = g.ny * g.nz;
-        ux = V2(a.u_face[fi], a.u_face[fi + 1]);
-        uy = V2(a.u_face[fn + fi], a.u_face[fn + fi + 1]);
-        uz = V2(a.u_face[2 * fn + fi], a.u_face[2 * fn + fi + 1]);
-      }
-      zou_he_inlet_T<V2>(mu, ux, uy, uz);
-    }
-  }
+  // (x faces are listed pairs: no Zou-He transpose here)
 #pragma unroll
   for (int i = 0; i < Q; ++i) *reinterpret_cast<float2*>(P.out[i] + idx) = mu[i].v;
   return gr;
@@ -443,8 +430,8 @@ __device__ __forceinline__ void adjoint_pair_list_part(const AdjPairArgs<St>& P,
   const Grid& g = A.s.g;
   const int t = nlist_block * blockDim.x + threadIdx.x;
   double gr = 0.0;
-  if (t < 2 * A.s.spec_adj_count)
-    gr = adjoint_cell<St, MRT>(A, (__ldg(A.s.spec_adj + (t >> 1)) << 1) + (t & 1));
+  if (t < 2 * A.s.spec_count)
+    gr = adjoint_cell<St, MRT>(A, (__ldg(A.s.spec_pairs + (t >> 1)) << 1) + (t & 1));
 #pragma unroll
   for (int o = 16; o > 0; o >>= 1) gr += __shfl_down_sync(0xffffffffu, gr, o);
   // slots after the nblocks * 8 per-cell ones; one per warp (at most n / 32
@@ -470,7 +457,7 @@ __device__ __forceinline__ double adjoint_pair_interior(const AdjPairArgs<St>& P
   decode(g, idx, x, y, z);
   const uint32_t t0 = a.tag ? __ldg(a.tag + idx) : 0u;
   const uint32_t t1 = a.tag ? __ldg(a.tag + idx + 1) : 0u;
-  if (pair_special(g, a.near, sizeof(St) == 2, true, x, y, z, t0, t1)) return 0.0;
+  if (pair_special(g, a.near, sizeof(St) == 2, x, y, z, t0, t1)) return 0.0;
   const int cls = sizeof(St) == 2 ? near_class(g, a.near, x, y, z, 2) : 0;
   V2 mu[Q], f[Q];
   const int nyz = g.ny * g.nz;
@@ -629,7 +616,7 @@ cudaError_t launch_adjoint(const AdjArgs<typename Storage<St>::Re>& A, bool mrt,
   // against 280 / 265 us for k_adjoint); SOFT for a porosity blend
   if constexpr (sizeof(typename Storage<St>::Re) == 4) {
     const Grid& g = A.s.g;
-    if ((g.nz % 2) == 0 && A.s.spec_adj) {
+    if ((g.nz % 2) == 0 && A.s.spec_pairs) {
       AdjPairArgs<St> P;
       P.A = A;
       const long long N = g.n, nyz = (long long)g.ny * g.nz;
@@ -642,7 +629,7 @@ cudaError_t launch_adjoint(const AdjArgs<typename Storage<St>::Re>& A, bool mrt,
         P.soff2[1][i] = make_float2(A.s.soff_near[i], A.s.soff_near[i]);
       }
       const int nb = (g.n / 2 + kAdjPairBlock - 1) / kAdjPairBlock;
-      const int nlist = (2 * A.s.spec_adj_count + kAdjPairBlock - 1) / kAdjPairBlock;
+      const int nlist = (2 * A.s.spec_count + kAdjPairBlock - 1) / kAdjPairBlock;
       const bool soft = (A.s.flags & (SF_SOLID_SPHERE | SF_SOLID_FIELD)) != 0;
       if (mrt && soft)
         k_adjoint_pair<St, true, true><<<nlist + nb, kAdjPairBlock, 0, st>>>(P, nlist);
@@ -763,7 +750,7 @@ __global__ void __launch_bounds__(kAdjPairBlock, LBM_ADJ_PAIR_BATCH_MINB)
     }
   }
   __syncthreads();
-  const int nlist = (2 * P.A.s.spec_adj_count + kAdjPairBlock - 1) / kAdjPairBlock;
+  const int nlist = (2 * P.A.s.spec_count + kAdjPairBlock - 1) / kAdjPairBlock;
   const int nint = (P.A.s.g.n / 2 + kAdjPairBlock - 1) / kAdjPairBlock;
   const int end = m.y + kBatchChunk < nlist + nint ? m.y + kBatchChunk : nlist + nint;
   for (int sb = m.y; sb < end; ++sb) {

@@ -146,7 +146,7 @@ void drop_graph(lbm_batch* b);
 int build_pmaps(lbm_batch* b) {
   b->pair_adjoint = true;
   for (auto* s : b->sims)
-    if ((s->g.nz % 2) != 0 || !s->spec_adj) b->pair_adjoint = false;
+    if ((s->g.nz % 2) != 0 || !s->spec_pairs) b->pair_adjoint = false;
   if (!b->pair_adjoint) return LBM_OK;
   std::vector<int> order(b->count);
   for (int i = 0; i < b->count; ++i) order[i] = i;
@@ -156,7 +156,7 @@ int build_pmaps(lbm_batch* b) {
   for (int i : order) {
     const lbm_sim* s = b->sims[i];
     const int soft = (s->porosity_mode == LBM_POROSITY_SOFT) ? 1 : 0;
-    const int nlist = (2 * s->nspec_adj + kPairBlock - 1) / kPairBlock;
+    const int nlist = (2 * s->nspec + kPairBlock - 1) / kPairBlock;
     const int nint = int((s->n / 2 + kPairBlock - 1) / kPairBlock);
     for (int j = 0; j < nlist + nint; j += kBatchChunk) map[soft].push_back(make_int2(i, j));
   }

@@ -92,9 +92,8 @@ void free_geometry(lbm_sim* s) {
   cudaFree(s->rec);
   cudaFree(s->porosity);
   cudaFree(s->spec_pairs);
-  cudaFree(s->spec_adj);
-  s->spec_pairs = s->spec_adj = nullptr;
-  s->nspec = s->nspec_adj = 0;
+  s->spec_pairs = nullptr;
+  s->nspec = 0;
   s->tag = nullptr;
   s->rec = nullptr;
   s->porosity = nullptr;
@@ -108,9 +107,8 @@ void free_geometry(lbm_sim* s) {
 // Only for even nz (the pair kernels' condition).
 int build_pair_list(lbm_sim* s, cudaStream_t st) {
   cudaFree(s->spec_pairs);
-  cudaFree(s->spec_adj);
-  s->spec_pairs = s->spec_adj = nullptr;
-  s->nspec = s->nspec_adj = 0;
+  s->spec_pairs = nullptr;
+  s->nspec = 0;
   if (s->g.nz % 2 != 0 || s->p.storage == LBM_F64) return LBM_OK;
   const int np = s->g.n / 2;
   const int use_class = (s->p.storage == LBM_F16 || s->p.storage == LBM_BF16) ? 1 : 0;
@@ -123,26 +121,19 @@ int build_pair_list(lbm_sim* s, cudaStream_t st) {
   if (!rc) rc = cuda_check(cudaStreamSynchronize(st), "sync");
   cudaFree(flags);
   if (rc) return rc;
-  for (int which = 0; which < 2; ++which) {
-    std::vector<int> list;
-    for (int p = 0; p < np; ++p)
-      if (h[p] & (1u << which)) list.push_back(p);
-    int* d = nullptr;
-    LBM_TRY(dev_alloc((void**)&d, (list.empty() ? 1 : list.size()) * sizeof(int)));
-    if (!list.empty() &&
-        (rc = cuda_check(cudaMemcpy(d, list.data(), list.size() * sizeof(int),
-                                    cudaMemcpyHostToDevice), "list H2D"))) {
-      cudaFree(d);
-      return rc;
-    }
-    if (which == 0) {
-      s->spec_pairs = d;
-      s->nspec = int(list.size());
-    } else {
-      s->spec_adj = d;
-      s->nspec_adj = int(list.size());
-    }
+  std::vector<int> list;
+  for (int p = 0; p < np; ++p)
+    if (h[p]) list.push_back(p);
+  int* d = nullptr;
+  LBM_TRY(dev_alloc((void**)&d, (list.empty() ? 1 : list.size()) * sizeof(int)));
+  if (!list.empty() &&
+      (rc = cuda_check(cudaMemcpy(d, list.data(), list.size() * sizeof(int),
+                                  cudaMemcpyHostToDevice), "list H2D"))) {
+    cudaFree(d);
+    return rc;
   }
+  s->spec_pairs = d;
+  s->nspec = int(list.size());
   return LBM_OK;
 }
 

@@ -121,10 +121,8 @@ template <class Re> struct StepArgs {
   Re soff[Q];             // outside the box
   Re soff_near[Q];        // inside the box
   int near[6];            // [x0, x1) x [y0, y1) x [z0, z1); empty when x0 >= x1
-  const int* spec_pairs;  // pairs the forward pair kernel runs on its per-cell path (nz even)
+  const int* spec_pairs;  // pairs the pair kernels run on their per-cell path (nz even)
   int spec_count;
-  const int* spec_adj;    // the same for the adjoint pair kernel (x faces included)
-  int spec_adj_count;
   double* force_partials; // [gridDim.x][3]
   unsigned long long* guard_count;
 };
@@ -182,18 +180,17 @@ __device__ __forceinline__ int near_class(const Grid& g, const int b[6], int x, 
 }
 
 // A z-pair (z even) that the packed pair kernels run on their per-cell path:
-// a boundary record on either cell, a non-periodic y/z edge, an x face
-// (adjoint pair kernel), or
-// (when the storage offsets matter, use_class) a neighbourhood that straddles
-// the body box.  The pair kernels' interior blocks skip these pairs; their
-// list blocks compute them from the list built with this same predicate.
+// a boundary record on either cell, an x face (fallback pull and Zou-He), a
+// non-periodic y/z edge, or (when the storage offsets matter, use_class) a
+// neighbourhood that straddles the body box.  The pair kernels' interior
+// blocks skip these pairs; their list blocks compute them from the list built
+// with this same predicate.  (Listing the x faces rather than testing for
+// them in the interior measured 94 us against 100 us per 16-bit step at
+// 256x128x128.)
 __device__ __forceinline__ bool pair_special(const Grid& g, const int near[6], bool use_class,
-                                             bool faces, int x, int y, int z, uint32_t t0,
-                                             uint32_t t1) {
-  // x faces: packed in the forward pair kernel unless the grid is too thin,
-  // listed (faces) for the adjoint pair kernel
+                                             int x, int y, int z, uint32_t t0, uint32_t t1) {
   const bool xface = x == 0 || x == g.nx - 1;
-  bool sp = ((t0 | t1) & TAG_INDEX) || (xface && (faces || g.nx < 3));
+  bool sp = ((t0 | t1) & TAG_INDEX) || xface;
   if (!g.periodic_yz) sp = sp || y == 0 || y == g.ny - 1 || z == 0 || z + 2 == g.nz;
   if (use_class && !sp) sp = near_class(g, near, x, y, z, 2) == 2;
   return sp;

@@ -91,10 +91,8 @@ struct lbm_sim {
   int nlinks = 0;
   double area = 0.0;
   int near[6] = {0, 0, 0, 0, 0, 0};   // rest-offset box of 16-bit storage (solid bbox + 2)
-  int* spec_pairs = nullptr;          // pairs the forward pair kernel runs per cell
+  int* spec_pairs = nullptr;          // pairs the pair kernels run per cell (pair_special)
   int nspec = 0;
-  int* spec_adj = nullptr;            // pairs the adjoint pair kernel runs per cell
-  int nspec_adj = 0;
   int have_geometry = 0;
   int porosity_mode = LBM_POROSITY_NONE;
   int sphere_porosity = 0;   // analytic sigmoid porosity in-kernel
@@ -176,8 +174,6 @@ inline void fill_args(const lbm_sim* s, StepArgs<Re>& a) {
   for (int k = 0; k < 6; ++k) a.near[k] = s->near[k];
   a.spec_pairs = s->spec_pairs;
   a.spec_count = s->nspec;
-  a.spec_adj = s->spec_adj;
-  a.spec_adj_count = s->nspec_adj;
   // guard reset targets: pre -> f_eq(1, (U,0,0)) (examples/10:160), post -> f_eq(1, 0) = w
   for (int i = 0; i < Q; ++i) {
     if (s->p.guard == LBM_GUARD_PRE) {

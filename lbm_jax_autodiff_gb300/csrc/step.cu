@@ -272,8 +272,9 @@ __device__ __forceinline__ void step_pair_list_part(const PairArgs<St>& P, int n
   add_resets(a, resets);
 }
 
-// Pull (packed, y/z wrap, x-face fallback and Zou-He) and finish of one
-// interior pair; CLS as for finish_pair, `cls` the tested class when CLS < 0.
+// Pull (packed, y wrap shared by both lanes, z wrap per lane) and finish of
+// one interior pair; CLS as for finish_pair, `cls` the tested class when
+// CLS < 0.  The x faces are listed pairs, so every source lies in the grid.
 template <class St, bool MRT, int CLS>
 __device__ __forceinline__ unsigned step_pair_interior(const PairArgs<St>& P, int idx, int x,
                                                        int y, int z, uint32_t t0, uint32_t t1,
@@ -283,41 +284,19 @@ __device__ __forceinline__ unsigned step_pair_interior(const PairArgs<St>& P, in
   const Grid& g = a.g;
   if (CLS >= 0) cls = CLS;
   V2 f[Q];
-  {
-    // y wrap shared by both lanes, z wrap per lane; on the x faces the
-    // directions whose source lies outside keep the cell's own value
-    // (streaming.py:123-131)
-    const int nyz = g.ny * g.nz;
-    const int iym = idx + (y == 0 ? nyz : 0);          // e_y = +1 pulls y - 1
-    const int iyp = idx - (y == g.ny - 1 ? nyz : 0);   // e_y = -1 pulls y + 1
-    const int zw0 = z == 0 ? g.nz : 0;                 // lane 0, e_z = +1 pulls z - 1
-    const int zw1 = z + 2 == g.nz ? -g.nz : 0;         // lane 1, e_z = -1 pulls z + 2
-    const int xlo = x == 0, xhi = x == g.nx - 1;
-    const size_t N = size_t(g.n);
+  const int nyz = g.ny * g.nz;
+  const int iym = idx + (y == 0 ? nyz : 0);          // e_y = +1 pulls y - 1
+  const int iyp = idx - (y == g.ny - 1 ? nyz : 0);   // e_y = -1 pulls y + 1
+  const int zw0 = z == 0 ? g.nz : 0;                 // lane 0, e_z = +1 pulls z - 1
+  const int zw1 = z + 2 == g.nz ? -g.nz : 0;         // lane 1, e_z = -1 pulls z + 2
 #pragma unroll
-    for (int i = 0; i < Q; ++i) {
-      const V2 so(P.soff2[cls][i]);
-      if ((ex(i) == 1 && xlo) || (ex(i) == -1 && xhi)) {
-        f[i] = Pr::ld2(static_cast<const St*>(a.src) + i * N + idx, so);
-        continue;
-      }
-      const int b = ey(i) == 1 ? iym : (ey(i) == -1 ? iyp : idx);
-      const St* p = P.pull[i] + b;
-      if (ez(i) == 0) f[i] = Pr::ld2(p, so);
-      else if (ez(i) == 1) f[i] = Pr::ld2s(p + zw0, p + 1, so);
-      else f[i] = Pr::ld2s(p, p + 1 + zw1, so);
-    }
-    if (xlo && !(a.flags & SF_NO_INLET)) {
-      V2 ux(a.u_in[0]), uy(a.u_in[1]), uz(a.u_in[2]);
-      if (a.flags & SF_INLET_FACE) {
-        const int fi = y * g.nz + z, fn = g.ny * g.nz;
-        ux = V2(a.u_face[fi], a.u_face[fi + 1]);
-        uy = V2(a.u_face[fn + fi], a.u_face[fn + fi + 1]);
-        uz = V2(a.u_face[2 * fn + fi], a.u_face[2 * fn + fi + 1]);
-      }
-      zou_he_inlet<V2>(f, ux, uy, uz);
-    }
-    if (xhi && !(a.flags & SF_NO_OUTLET)) zou_he_outlet<V2>(f, V2(a.rho_out));
+  for (int i = 0; i < Q; ++i) {
+    const V2 so(P.soff2[cls][i]);
+    const int b = ey(i) == 1 ? iym : (ey(i) == -1 ? iyp : idx);
+    const St* p = P.pull[i] + b;
+    if (ez(i) == 0) f[i] = Pr::ld2(p, so);
+    else if (ez(i) == 1) f[i] = Pr::ld2s(p + zw0, p + 1, so);
+    else f[i] = Pr::ld2s(p, p + 1 + zw1, so);
   }
   return finish_pair<St, MRT, CLS>(P, idx, x, y, z, t0, t1, f);
 }
@@ -352,7 +331,7 @@ __global__ void __launch_bounds__(kPairBlock, LBM_STEP_PAIR_MINB) k_step_pair(co
     t0 = a.tag ? __ldg(a.tag + idx) : 0u;
     t1 = a.tag ? __ldg(a.tag + idx + 1) : 0u;
     // listed pairs run in the list blocks
-    active = !pair_special(g, a.near, sizeof(St) == 2, false, x, y, z, t0, t1);
+    active = !pair_special(g, a.near, sizeof(St) == 2, x, y, z, t0, t1);
   }
   // storage offset class per pair (0 outside the body box, 1 inside; listed
   // pairs straddle it).  FP16: a warp whose pairs are all outside runs a
@@ -371,8 +350,7 @@ __global__ void __launch_bounds__(kPairBlock, LBM_STEP_PAIR_MINB) k_step_pair(co
   add_resets(a, resets);
 }
 
-// Per pair: bit 0 if pair_special for the forward pair kernel, bit 1 for the
-// adjoint pair kernel (the kernels' own skip tests).
+// Per pair: 1 if pair_special (the pair kernels' own skip test), else 0.
 __global__ void k_pair_flags(Grid g, const uint32_t* __restrict__ tag, Near nb, int use_class,
                              uint8_t* __restrict__ flags) {
   const int p = blockIdx.x * blockDim.x + threadIdx.x;
@@ -381,8 +359,7 @@ __global__ void k_pair_flags(Grid g, const uint32_t* __restrict__ tag, Near nb, 
   int x, y, z;
   decode(g, idx, x, y, z);
   const uint32_t t0 = tag ? tag[idx] : 0u, t1 = tag ? tag[idx + 1] : 0u;
-  flags[p] = (pair_special(g, nb.b, use_class != 0, false, x, y, z, t0, t1) ? 1 : 0) |
-             (pair_special(g, nb.b, use_class != 0, true, x, y, z, t0, t1) ? 2 : 0);
+  flags[p] = pair_special(g, nb.b, use_class != 0, x, y, z, t0, t1) ? 1 : 0;
 }
 
 cudaError_t launch_pair_flags(const Grid& g, const uint32_t* tag, const int near[6], int use_class,
