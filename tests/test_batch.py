@@ -146,3 +146,24 @@ def test_autotune_and_block_shapes(cuda):
     assert block in (128, 256) and 1 <= K <= 200
     assert b.plan[0] == block and b.plan[1] == K
     b.close()
+
+
+def test_geometry_change_between_replays(cuda):
+    """New radii rebuild the instances' boundary lists and the pair-adjoint
+    block maps under an already captured graph: the replay equals a fresh
+    batch at the new radii, and the graph holds the planned launches."""
+    n, K = 30, 10
+    b = _batch()
+    b.cd_and_grad(n, checkpoint_every=K, use_graph=True)      # capture
+    sph2 = [dict(s, radius=s["radius"] + 0.15) for s in SPH]
+    b.set_spheres(sph2)
+    cd, g = b.cd_and_grad(n, checkpoint_every=K, use_graph=True)
+    b2 = _batch(sph=sph2)
+    cd2, g2 = b2.cd_and_grad(n, checkpoint_every=K, use_graph=False)
+    assert np.array_equal(cd, cd2) and np.array_equal(g, g2)
+    # n forward + stream/force + finalize + zero + seed + (n - K) recompute
+    # + n adjoint steps x 2 launches (instances without / with a porosity
+    # blend) + reduce
+    assert b.graph_launches == n + 4 + (n - K) + 2 * n + 1
+    b.close()
+    b2.close()
