@@ -91,10 +91,15 @@ template <> struct Pair<float> {
     *reinterpret_cast<float2*>(p) = v.v;
   }
 };
-// float(h) + c for a bfloat16 h in one mixed-precision add (sm_100+); the
+// float(h) + c for a 16-bit h in one mixed-precision add (sm_100+); the
 // conversion is exact, so this rounds as convert-then-add does.  (Measured
-// 98 us against 104 us per bf16 step at 256x128x128; for fp16 storage the
-// plain convert-then-add form measured faster.)
+// 98 us against 104 us per bf16 step at 256x128x128, 91.1 us against 92.1 us
+// per fp16 step.)
+__device__ __forceinline__ float add_f16(__half h, float c) {
+  float d;
+  asm("add.rn.f32.f16 %0, %1, %2;" : "=f"(d) : "h"(__half_as_ushort(h)), "f"(c));
+  return d;
+}
 __device__ __forceinline__ float add_bf16(__nv_bfloat16 h, float c) {
   float d;
   asm("add.rn.f32.bf16 %0, %1, %2;" : "=f"(d) : "h"(__bfloat16_as_ushort(h)), "f"(c));
@@ -103,10 +108,11 @@ __device__ __forceinline__ float add_bf16(__nv_bfloat16 h, float c) {
 
 template <> struct Pair<__half> {
   static __device__ __forceinline__ V2 ld2(const __half* p, V2 w) {
-    return V2(__half22float2(ldg_s(reinterpret_cast<const __half2*>(p)))) + w;
+    const __half2 v = ldg_s(reinterpret_cast<const __half2*>(p));
+    return V2(add_f16(__low2half(v), w.x()), add_f16(__high2half(v), w.y()));
   }
   static __device__ __forceinline__ V2 ld2s(const __half* p0, const __half* p1, V2 w) {
-    return V2(__half22float2(__halves2half2(ldg_s(p0), ldg_s(p1)))) + w;
+    return V2(add_f16(ldg_s(p0), w.x()), add_f16(ldg_s(p1), w.y()));
   }
   static __device__ __forceinline__ void st2(__half* p, V2 v, V2 w) {
     *reinterpret_cast<__half2*>(p) = __float22half2_rn((v - w).v);
