@@ -245,11 +245,9 @@ __device__ __forceinline__ double adjoint_cell(const AdjArgs<typename Storage<St
     const bool hard = (fl & SF_SOLID_HARD) && (tag & TAG_SOLID);
     Re p = Re(0);
     if (soft) {
-      Re dpdr = Re(0);
-      if (fl & SF_SOLID_SPHERE)
-        p = sphere_porosity<Re>(a.sph, x, y, z, &dpdr);
-      else
-        p = a.porosity[idx];
+      // porosity field, or the sigmoid sphere's precomputed p and dp/dr
+      p = a.porosity[idx];
+      const Re dpdr = (fl & SF_SOLID_SPHERE) ? a.dpdr[idx] : Re(0);
       // dJ/dr gets mu . dB/dp dp/dr; dp/dr = alpha p (1 - p) is below
       // alpha 2^-40 (2^-70 in FP64) outside a shell a few cells thick around
       // the surface, 4e-12 of its peak alpha / 4, so the collision recompute
@@ -371,11 +369,11 @@ __device__ __forceinline__ double adj_pair_finish(const AdjPairArgs<St>& P, int 
     // S = (1 - p) c + p c_opp per lane (smooth.py:118-155).  A sigmoid
     // sphere adds dJ/dr += mu . (c_opp - c) dp/dr, skipped where dp/dr <
     // alpha 2^-40 as in adjoint_cell
-    V2 p;
+    // porosity field, or the sigmoid sphere's precomputed p and dp/dr
+    const V2 p(__ldg(reinterpret_cast<const float2*>(a.porosity + idx)));
     if (fl & SF_SOLID_SPHERE) {
-      float d0, d1;
-      p = V2(sphere_porosity<float>(a.sph, x, y, z, &d0),
-             sphere_porosity<float>(a.sph, x, y, z + 1, &d1));
+      const float2 dd = __ldg(reinterpret_cast<const float2*>(a.dpdr + idx));
+      const float d0 = dd.x, d1 = dd.y;
       const float thr = a.sph.alpha * 9.094947017729282e-13f;
       const bool n0 = d0 > thr, n1 = d1 > thr;
       if (n0 || n1) {
@@ -386,8 +384,6 @@ __device__ __forceinline__ double adj_pair_finish(const AdjPairArgs<St>& P, int 
         if (n0) gr += double(gp.x()) * double(d0);
         if (n1) gr += double(gp.y()) * double(d1);
       }
-    } else {
-      p = V2(__ldg(reinterpret_cast<const float2*>(a.porosity + idx)));
     }
     const V2 omp = V2(1.0f) - p;
     V2 m2[Q];

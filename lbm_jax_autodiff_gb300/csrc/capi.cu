@@ -91,12 +91,13 @@ void free_geometry(lbm_sim* s) {
   cudaFree(s->tag);
   cudaFree(s->rec);
   cudaFree(s->porosity);
+  cudaFree(s->dpdr);
   cudaFree(s->spec_pairs);
   s->spec_pairs = nullptr;
   s->nspec = 0;
   s->tag = nullptr;
   s->rec = nullptr;
-  s->porosity = nullptr;
+  s->porosity = s->dpdr = nullptr;
   s->nrec = 0;
   s->nlinks = 0;
   s->have_geometry = 0;
@@ -385,11 +386,24 @@ int lbm_set_geometry_sphere(lbm_sim* s, const lbm_sphere* sp, void* stream) {
     return set_error(LBM_ERR_ARG, "lbm_set_geometry_sphere: bad enum");
   cudaStream_t st = static_cast<cudaStream_t>(stream);
   cudaFree(s->porosity);
-  s->porosity = nullptr;
+  cudaFree(s->dpdr);
+  s->porosity = s->dpdr = nullptr;
   s->sphere = *sp;
   s->porosity_mode = sp->porosity;
   s->sphere_porosity = sp->porosity == LBM_POROSITY_SOFT;
-  return is_fp64(s) ? set_sphere_impl<double>(s, sp, st) : set_sphere_impl<float>(s, sp, st);
+  LBM_TRY(is_fp64(s) ? set_sphere_impl<double>(s, sp, st) : set_sphere_impl<float>(s, sp, st));
+  if (!s->sphere_porosity) return LBM_OK;
+  // sigmoid sphere: porosity and dp/dr fields for the kernels
+  LBM_TRY(dev_alloc(&s->porosity, s->n * s->re_bytes));
+  LBM_TRY(dev_alloc(&s->dpdr, s->n * s->re_bytes));
+  const cudaError_t e =
+      is_fp64(s) ? launch_sphere_porosity<double>(s->g, sphere_params<double>(s),
+                                                  static_cast<double*>(s->porosity),
+                                                  static_cast<double*>(s->dpdr), st)
+                 : launch_sphere_porosity<float>(s->g, sphere_params<float>(s),
+                                                 static_cast<float*>(s->porosity),
+                                                 static_cast<float*>(s->dpdr), st);
+  return cuda_check(e, "sphere porosity");
 }
 
 int lbm_set_geometry_mask(lbm_sim* s, const int32_t* solid, const void* q, double default_q,
@@ -400,7 +414,8 @@ int lbm_set_geometry_mask(lbm_sim* s, const int32_t* solid, const void* q, doubl
   LBM_TRY(check_align(porosity, s->re_bytes, "porosity"));
   cudaStream_t st = static_cast<cudaStream_t>(stream);
   cudaFree(s->porosity);
-  s->porosity = nullptr;
+  cudaFree(s->dpdr);
+  s->porosity = s->dpdr = nullptr;
   s->sphere_porosity = 0;
   if (porosity) {
     LBM_TRY(dev_alloc(&s->porosity, s->n * s->re_bytes));

@@ -292,6 +292,32 @@ cudaError_t launch_area_cols(const Grid& g, const uint8_t* solid, int* col, cuda
   return cudaGetLastError();
 }
 
+// Per-cell porosity and dp/dr of a sigmoid sphere (sphere_porosity), once per
+// geometry: the step and adjoint kernels read them instead of evaluating the
+// sigmoid (three divisions, a square root and an exponential) every step.
+template <class Re>
+__global__ void k_sphere_porosity(Grid g, SphereP<Re> sp, Re* __restrict__ p,
+                                  Re* __restrict__ dpdr) {
+  const int idx = blockIdx.x * blockDim.x + threadIdx.x;
+  if (idx >= g.n) return;
+  int x, y, z;
+  decode(g, idx, x, y, z);
+  Re d;
+  p[idx] = sphere_porosity<Re>(sp, x, y, z, &d);
+  dpdr[idx] = d;
+}
+
+template <class Re>
+cudaError_t launch_sphere_porosity(const Grid& g, const SphereP<Re>& sp, Re* p, Re* dpdr,
+                                   cudaStream_t st) {
+  k_sphere_porosity<Re><<<(g.n + 255) / 256, 256, 0, st>>>(g, sp, p, dpdr);
+  return cudaGetLastError();
+}
+
+template cudaError_t launch_sphere_porosity<float>(const Grid&, const SphereP<float>&, float*,
+                                                   float*, cudaStream_t);
+template cudaError_t launch_sphere_porosity<double>(const Grid&, const SphereP<double>&, double*,
+                                                    double*, cudaStream_t);
 template cudaError_t launch_sphere_fields<float>(const Grid&, const SphereSpec&, uint8_t*, float*,
                                                  float*, cudaStream_t);
 template cudaError_t launch_sphere_fields<double>(const Grid&, const SphereSpec&, uint8_t*,

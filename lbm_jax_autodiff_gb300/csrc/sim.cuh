@@ -113,7 +113,8 @@ template <class Re> struct StepArgs {
   const Re* u_face;       // [3][ny][nz]
   Re rho_out;
   SphereP<Re> sph;
-  const Re* porosity;     // [n]
+  const Re* porosity;     // [n] porosity field (also filled for a sigmoid sphere)
+  const Re* dpdr;         // [n] dp/dr of a sigmoid sphere, else null
   Re guard_reset[Q];
   // 16-bit storage holds f_i minus an offset: the rest equilibrium w_i inside
   // the box `near` around the body (where u ~ 0), the free-stream equilibrium

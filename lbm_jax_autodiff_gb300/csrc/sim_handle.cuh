@@ -30,6 +30,9 @@ template <class Re>
 cudaError_t launch_sphere_fields(const Grid& g, const SphereSpec& s, uint8_t* solid, Re* q,
                                  Re* dqdr, cudaStream_t st);
 template <class Re>
+cudaError_t launch_sphere_porosity(const Grid& g, const SphereP<Re>& sp, Re* p, Re* dpdr,
+                                   cudaStream_t st);
+template <class Re>
 cudaError_t launch_q_from_solid(const Grid& g, const uint8_t* solid, double dq, Re* q,
                                 cudaStream_t st);
 cudaError_t launch_solid_from_i32(int n, const int32_t* m, uint8_t* s, cudaStream_t st);
@@ -98,6 +101,7 @@ struct lbm_sim {
   int sphere_porosity = 0;   // analytic sigmoid porosity in-kernel
   lbm_sphere sphere{};
   void* porosity = nullptr;  // porosity field (compute dtype)
+  void* dpdr = nullptr;      // dp/dr field of a sigmoid sphere (compute dtype)
   void* u_face = nullptr;    // inlet profile (compute dtype)
   double* partials = nullptr;
   int nblocks = 0;
@@ -134,6 +138,23 @@ inline void fill_consts(const lbm_params& p, Consts<Re>& K) {
   }
 }
 
+// Sigmoid-sphere parameters in the kernels' arithmetic type (world frame:
+// x in [-4, 4], y and z in [-2, 2]); the precomputed porosity fields and the
+// kernels' arguments use the same values.
+template <class Re>
+inline SphereP<Re> sphere_params(const lbm_sim* s) {
+  SphereP<Re> p;
+  p.c[0] = Re(s->sphere.center[0]);
+  p.c[1] = Re(s->sphere.center[1]);
+  p.c[2] = Re(s->sphere.center[2]);
+  p.r = Re(s->sphere.radius);
+  p.alpha = Re(s->sphere.sharpness);
+  p.sx = Re(s->g.nx / 8.0);
+  p.sy = Re(s->g.ny / 4.0);
+  p.sz = Re(s->g.nz / 4.0);
+  return p;
+}
+
 template <class Re>
 inline void fill_args(const lbm_sim* s, StepArgs<Re>& a) {
   memset(&a, 0, sizeof(a));
@@ -154,15 +175,9 @@ inline void fill_args(const lbm_sim* s, StepArgs<Re>& a) {
   for (int k = 0; k < 3; ++k) a.u_in[k] = Re(s->p.inlet_velocity[k]);
   a.u_face = static_cast<const Re*>(s->u_face);
   a.rho_out = Re(s->p.rho_out);
-  a.sph.c[0] = Re(s->sphere.center[0]);
-  a.sph.c[1] = Re(s->sphere.center[1]);
-  a.sph.c[2] = Re(s->sphere.center[2]);
-  a.sph.r = Re(s->sphere.radius);
-  a.sph.alpha = Re(s->sphere.sharpness);
-  a.sph.sx = Re(s->g.nx / 8.0);
-  a.sph.sy = Re(s->g.ny / 4.0);
-  a.sph.sz = Re(s->g.nz / 4.0);
+  a.sph = sphere_params<Re>(s);
   a.porosity = static_cast<const Re*>(s->porosity);
+  a.dpdr = static_cast<const Re*>(s->dpdr);
   // 16-bit storage offsets: the rest equilibrium w inside the box around the
   // body, the free-stream equilibrium f_eq(1, (U, 0, 0)) elsewhere
   for (int i = 0; i < Q; ++i) {

@@ -115,8 +115,7 @@ __device__ __forceinline__ void step_body(const StepArgs<typename Storage<St>::R
         for (int i = 0; i < Q; ++i)
           S::st(dst + i * N + idx, c[opp(i)], nr ? a.soff_near[i] : a.soff[i]);
       } else if (fl & (SF_SOLID_SPHERE | SF_SOLID_FIELD)) {
-        const Re p = (fl & SF_SOLID_SPHERE) ? sphere_porosity<Re>(a.sph, x, y, z, nullptr)
-                                            : a.porosity[idx];
+        const Re p = a.porosity[idx];   // field, or the sigmoid sphere's precomputed one
         const Re omp = Re(1) - p;
 #pragma unroll
         for (int i = 0; i < Q; ++i)
@@ -211,12 +210,8 @@ __device__ __forceinline__ unsigned finish_pair(const PairArgs<St>& P, int idx, 
       Pr::st2(out[i] + idx, V2(s0 ? c[opp(i)].x() : c[i].x(), s1 ? c[opp(i)].y() : c[i].y()),
               off(i));
   } else if (fl & (SF_SOLID_SPHERE | SF_SOLID_FIELD)) {
-    V2 p;
-    if (fl & SF_SOLID_SPHERE)
-      p = V2(sphere_porosity<float>(a.sph, x, y, z, nullptr),
-             sphere_porosity<float>(a.sph, x, y, z + 1, nullptr));
-    else
-      p = V2(__ldg(reinterpret_cast<const float2*>(a.porosity + idx)));
+    // porosity field, or the sigmoid sphere's precomputed one
+    const V2 p(__ldg(reinterpret_cast<const float2*>(a.porosity + idx)));
     const V2 omp = V2(1.0f) - p;
 #pragma unroll
     for (int i = 0; i < Q; ++i) Pr::st2(out[i] + idx, omp * c[i] + p * c[opp(i)], off(i));
