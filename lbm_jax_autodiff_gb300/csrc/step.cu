@@ -400,7 +400,7 @@ __global__ void k_force_finalize(const double* __restrict__ part, int nblocks, d
 
 // FP32 storage runs k_step, the fastest form for it when measured at
 // 256x128x128 (113-114 us vs 115-117 us for k_step_pair); 16-bit storage runs
-// k_step_pair (107-109 us vs ~117 us), the pair layout halving its
+// k_step_pair (91-92 us vs ~117 us for k_step), the pair layout halving its
 // conversion and address work per cell.
 template <class St>
 cudaError_t launch_step(const StepArgs<typename Storage<St>::Re>& a, bool mrt,
