@@ -703,7 +703,7 @@ __global__ void __launch_bounds__(256, LBM_ADJ_BATCH_MINB)
 
 // Batched k_adjoint_pair (FP32 storage, nz even): map[b] = (instance, first
 // sub-block), the sub-blocks of an instance being its list blocks then its
-// interior blocks, kBatchChunk per block; entries with instance -1 pad the
+// interior blocks, kPairBatchChunk per block; entries with instance -1 pad the
 // map to the grid the launch (and a captured graph) was sized for.  SOFT:
 // the instances with a porosity blend.
 #ifndef LBM_ADJ_PAIR_BATCH_MINB
@@ -748,7 +748,7 @@ __global__ void __launch_bounds__(kAdjPairBlock, LBM_ADJ_PAIR_BATCH_MINB)
   __syncthreads();
   const int nlist = (2 * P.A.s.spec_count + kAdjPairBlock - 1) / kAdjPairBlock;
   const int nint = (P.A.s.g.n / 2 + kAdjPairBlock - 1) / kAdjPairBlock;
-  const int end = m.y + kBatchChunk < nlist + nint ? m.y + kBatchChunk : nlist + nint;
+  const int end = m.y + kPairBatchChunk < nlist + nint ? m.y + kPairBatchChunk : nlist + nint;
   for (int sb = m.y; sb < end; ++sb) {
     if (sb < nlist)
       adjoint_pair_list_part<float, MRT>(P, sb);

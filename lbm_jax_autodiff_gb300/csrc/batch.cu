@@ -140,7 +140,7 @@ int build_map(lbm_batch* b) {
 void drop_graph(lbm_batch* b);
 
 // Block maps of the pair adjoint from the instances' current adjoint lists:
-// per instance its list blocks then its interior blocks, kBatchChunk per map
+// per instance its list blocks then its interior blocks, kPairBatchChunk per map
 // entry, largest instances first.  A map only grows (padded with -1 entries)
 // so the grid of a captured graph stays valid; growth drops the graph.
 int build_pmaps(lbm_batch* b) {
@@ -158,7 +158,7 @@ int build_pmaps(lbm_batch* b) {
     const int soft = (s->porosity_mode == LBM_POROSITY_SOFT) ? 1 : 0;
     const int nlist = (2 * s->nspec + kPairBlock - 1) / kPairBlock;
     const int nint = int((s->n / 2 + kPairBlock - 1) / kPairBlock);
-    for (int j = 0; j < nlist + nint; j += kBatchChunk) map[soft].push_back(make_int2(i, j));
+    for (int j = 0; j < nlist + nint; j += kPairBatchChunk) map[soft].push_back(make_int2(i, j));
   }
   for (int m = 0; m < 2; ++m) {
     const int need = int(map[m].size());
