@@ -317,14 +317,10 @@ def _batch_rate(n_steps, barrier, max_over_ranks):
                     "rebuild on the host" % (n_steps, rec, n_steps)}
 
 
-def run_ours(args):
+def rank_ops(dist, device):
+    """(barrier, max_over_ranks) over an initialised process group; dist None
+    for one rank.  Every timed figure is the maximum over ranks."""
     import torch
-    ws, rank, local = _dist()
-    torch.cuda.set_device(local)
-    dist = None
-    if ws > 1:
-        import torch.distributed as dist
-        dist.init_process_group("nccl")
 
     def barrier():
         if dist is not None:
@@ -333,9 +329,27 @@ def run_ours(args):
     def max_over_ranks(v):
         if dist is None:
             return v
-        t = torch.tensor([v], dtype=torch.float64, device="cuda")
+        t = torch.tensor([v], dtype=torch.float64, device=device)
         dist.all_reduce(t, op=dist.ReduceOp.MAX)
         return float(t.item())
+
+    return barrier, max_over_ranks
+
+
+def aggregate_mlups(ws, cells, steps, seconds):
+    """Whole-job MLUPS: every rank advances its own replica of `cells` cells."""
+    return ws * cells * steps / seconds / 1e6
+
+
+def run_ours(args):
+    import torch
+    ws, rank, local = _dist()
+    torch.cuda.set_device(local)
+    dist = None
+    if ws > 1:
+        import torch.distributed as dist
+        dist.init_process_group("nccl")
+    barrier, max_over_ranks = rank_ops(dist, "cuda")
 
     n_cells = NX * NY * NZ
     peak, peak_kind = _peaks()
@@ -347,7 +361,7 @@ def run_ours(args):
     t = _time_steps(sim, args.steps, args.warmup, barrier)
     clk = clocks.stop()
     t = max_over_ranks(t)
-    mlups = ws * n_cells * args.steps / t / 1e6
+    mlups = aggregate_mlups(ws, n_cells, args.steps, t)
     per_launch = t / args.steps
     achieved = BYTES_PER_UPDATE["fp32"] * n_cells / per_launch / 1e9
 
@@ -378,7 +392,7 @@ def run_ours(args):
     for _ in range(n_chunks):
         e2e_chunk()
     t_e2e = max_over_ranks(time.perf_counter() - t0)
-    e2e_mlups = ws * n_cells * chunk * n_chunks / t_e2e / 1e6
+    e2e_mlups = aggregate_mlups(ws, n_cells, chunk * n_chunks, t_e2e)
     state_bytes = 19 * n_cells * 4
     cd_last = float(cd_host[0, 3])
     sim.close()
@@ -390,7 +404,7 @@ def run_ours(args):
         t2 = max_over_ranks(_time_steps(s2, args.steps, args.warmup, barrier))
         s2.close()
         extra[storage] = {
-            "mlups": round(ws * n_cells * args.steps / t2 / 1e6, 1),
+            "mlups": round(aggregate_mlups(ws, n_cells, args.steps, t2), 1),
             "achieved_gbs": round(BYTES_PER_UPDATE[storage] * n_cells / (t2 / args.steps) / 1e9, 1),
             "frac": round(BYTES_PER_UPDATE[storage] * n_cells / (t2 / args.steps) / 1e9 / peak, 4),
         }
