@@ -255,3 +255,31 @@ def test_fp32_porosity_field_vs_fp64(cuda):
     scale = gq64.abs().max().item()
     assert scale > 0.0
     assert (gq32 - gq64).abs().max().item() <= 1e-3 * scale
+
+
+def test_full_size_precision_bars(cuda):
+    """The 256x128x128 workload (sphere D = 32, Re 100, MRT + Smagorinsky
+    Cs 0.1, Bouzidi hard sphere), dCd/dr over a 2000-step window, workspace
+    sized to free HBM: FP16 storage within 1e-3 and FP32 storage within
+    1e-4 (Cd) / 1e-5 (dCd/dr) of the FP64-storage solver."""
+    nx, ny, nz, n = 256, 128, 128, 2000
+    U = 0.05
+    tau = 3.0 * (U * 32.0 / 100.0) + 0.5
+
+    def run(st):
+        torch.cuda.empty_cache()
+        sim = _sim(nx, ny, nz, tau, storage=st, use_smagorinsky=True, smagorinsky_cs=0.1,
+                   inlet_velocity=(U, 0.0, 0.0))
+        sim.set_sphere(0.5, kind="dist", q_mode="bouzidi", porosity="hard")
+        sim.set_state(sim.equilibrium_state())
+        out = sim.cd_and_grad(n, checkpoint_every=0)
+        sim.close()
+        return out
+
+    cd64, g64 = run("fp64")
+    cd16, g16 = run("fp16")
+    cd32, g32 = run("fp32")
+    assert abs(cd16 - cd64) <= 1e-3 * abs(cd64), (cd16, cd64)
+    assert abs(g16 - g64) <= 1e-3 * abs(g64), (g16, g64)
+    assert abs(cd32 - cd64) <= 1e-4 * abs(cd64), (cd32, cd64)
+    assert abs(g32 - g64) <= 1e-5 * abs(g64), (g32, g64)
