@@ -331,10 +331,11 @@ __global__ void __launch_bounds__(256, sizeof(St) == 8 ? 1 : LBM_ADJ_MINB)
 
 // ---------------------------------------------------------------------------
 // k_adjoint_pair: the same adjoint step for two z-adjacent cells per thread
-// (FP32 storage, nz even, no porosity blend): the interior gather of
-// nu_{k+1}, the recomputed f_k and the collision transpose run on packed
-// float2 values (FP32x2 pipe).  Pairs with a boundary record, on an x face or
-// on a non-periodic y/z edge take the per-cell path of k_adjoint lane by lane.
+// (FP32 arithmetic, nz even): the interior gather of nu_{k+1}, the recomputed
+// f_k, the bounce-back or porosity-blend transpose and the collision transpose
+// run on packed float2 values (FP32x2 pipe).  Pairs with a boundary record, on
+// an x face, on a non-periodic y/z edge or (16-bit storage) straddling the
+// storage-offset box are listed and take the per-cell path of k_adjoint.
 // ---------------------------------------------------------------------------
 template <class St> struct AdjPairArgs {
   AdjArgs<float> A;
