@@ -20,8 +20,11 @@
 // arithmetic, nz even): the 19 populations of both cells live in packed
 // float2 registers and the collision runs on the FP32x2 pipe, the z-aligned
 // directions move as one 4-byte access of two 16-bit values, and the per-cell
-// index and conversion work is shared by the pair.  It serves 16-bit
-// storage; k_step serves FP32 / FP64, odd nz, the COLLIDE_ONLY / STREAM_ONLY
+// index and conversion work is shared by the pair; the pairs with a boundary
+// record, on an x face, on a non-periodic edge or straddling the storage-
+// offset box are listed and run lane by lane in the first blocks of the same
+// launch.  It serves 16-bit storage; k_step serves FP32 / FP64, odd nz, the
+// COLLIDE_ONLY / STREAM_ONLY
 // launches and the sampled steps that also sum the momentum-exchange force
 // (SF_FORCE).
 #include <type_traits>
