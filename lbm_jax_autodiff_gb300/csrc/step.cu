@@ -24,9 +24,8 @@
 // record, on an x face, on a non-periodic edge or straddling the storage-
 // offset box are listed and run lane by lane in the first blocks of the same
 // launch.  It serves 16-bit storage; k_step serves FP32 / FP64, odd nz, the
-// COLLIDE_ONLY / STREAM_ONLY
-// launches and the sampled steps that also sum the momentum-exchange force
-// (SF_FORCE).
+// COLLIDE_ONLY / STREAM_ONLY launches and the sampled steps that also sum the
+// momentum-exchange force (SF_FORCE).
 #include <type_traits>
 
 #include "batch.cuh"
