@@ -87,3 +87,16 @@ def test_create_rejects_bad_arguments_without_touching_the_gpu(lib):
     p.storage = 9
     assert L.lbm_create(ctypes.byref(p), ctypes.byref(h)) == nat.LBM_ERR_ARG
     assert L.lbm_create(None, ctypes.byref(h)) == nat.LBM_ERR_ARG
+
+
+def test_batch_entry_points_reject_null_handles(lib):
+    """The batch queries validate their arguments before any CUDA call."""
+    from lbm_jax_autodiff_gb300 import _native as nat
+    L = nat.load()
+    n = ctypes.c_longlong(-1)
+    assert L.lbm_batch_graph_launches(None, ctypes.byref(n)) == nat.LBM_ERR_ARG
+    assert n.value == -1
+    b, k, r = ctypes.c_int(), ctypes.c_int(), ctypes.c_int()
+    w, g = ctypes.c_ulonglong(), ctypes.c_double()
+    assert L.lbm_batch_get_plan(None, ctypes.byref(b), ctypes.byref(k), ctypes.byref(r),
+                                ctypes.byref(w), ctypes.byref(g)) == nat.LBM_ERR_ARG
