@@ -45,6 +45,14 @@ WORKLOAD = ("D3Q19 MRT+Smagorinsky(Cs=0.1) sphere D=32 Re=100, Bouzidi ray-spher
             "Zou-He in/out, periodic y/z, pre-collision guard, 256x128x128")
 
 
+def bench_config(ws):
+    """The workload description both arms print (the same dict, so the two
+    lines name the same configuration)."""
+    return {"workload": WORKLOAD, "grid": [NX, NY, NZ], "storage": "fp32",
+            "tau": round(TAU, 6), "l2": "inputs larger than L2 (A/B state 638 MB)",
+            "parallelism": "replicas" if ws > 1 else "single GPU"}
+
+
 def _peaks():
     try:
         with open(os.path.join(ROOT, "MEASURED_PEAKS.json")) as fh:
@@ -99,25 +107,28 @@ class ClockSampler:
             self.proc.wait(timeout=5)
         except Exception:
             self.proc.kill()
-        sm, mx, reasons = [], None, set()
+        rows, mx, reasons = [], None, set()
         names = ["hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap"]
         for ln in self.lines:
             p = [x.strip() for x in ln.split(",")]
             if len(p) < 9:
                 continue
             try:
-                sm.append(float(p[1]))
-                mx = float(p[2])
+                sm, mx, pw = float(p[1]), float(p[2]), float(p[3])
             except ValueError:
                 continue
-            for nm, v in zip(names, p[5:9]):
-                if v.lower() == "active":
-                    reasons.add(nm)
-        if not sm:
+            rows.append((sm, pw, [nm for nm, v in zip(names, p[5:9]) if v.lower() == "active"]))
+        if not rows:
             return None
-        sm.sort()
+        # under load: samples drawing at least 30 % of the highest power seen
+        pmax = max(r[1] for r in rows)
+        load = [r for r in rows if r[1] >= 0.3 * pmax] or rows
+        for r in load:
+            reasons.update(r[2])
+        sm = sorted(r[0] for r in load)
         return {"sm_mhz": sm[len(sm) // 2], "sm_max_mhz": mx, "reasons": sorted(reasons),
-                "samples": len(sm)}
+                "samples": len(rows), "samples_under_load": len(load),
+                "power_w_max": pmax, "window": "whole bench arm, sampled every 100 ms"}
 
 
 def _dist():
@@ -207,7 +218,7 @@ def run_reference(args):
         "ms_per_step": round(1e3 * dt / args.steps * NX / planes, 3),
         "higher_is_better": True, "scaling": "weak", "vs_baseline": None,
         "dtype": "f32", "data": "synthetic",
-        "config": {"workload": WORKLOAD, "grid": [NX, NY, NZ]},
+        "config": bench_config(ws),
         "cpu_baseline": {"value": round(mlups, 4), "unit": "MLUPS", "cores": threads,
                          "kind": "port", "sample": sample},
         "e2e": {"value": round(mlups, 4), "unit": "MLUPS", "h2d_bytes_per_step": 0,
@@ -304,7 +315,31 @@ def _batch_rate(n_steps, barrier, max_over_ranks):
     cells = b.cells
     b.close()
     torch.cuda.empty_cache()
+    # error against FP64 storage: the first n_check instances (both q modes,
+    # both porosity modes) re-evaluated alone in FP64 at the radius the timed
+    # iteration evaluated
+    from lbm_jax_autodiff_gb300 import Simulation
+    n_check = min(8, len(inst))
+    cd_err, g_err = [], []
+    for i in range(n_check):
+        p = dict(inst[i])
+        p["storage"] = "fp64"
+        nx, ny, nz = p.pop("nx"), p.pop("ny"), p.pop("nz")
+        tau = p.pop("tau")
+        s64 = Simulation(nx, ny, nz, tau, **p)
+        s64.set_sphere(**dict(sph[i], radius=float(h1["r"][0][i])))
+        s64.set_state(s64.equilibrium_state())
+        cd64, g64 = s64.cd_and_grad(n_steps, checkpoint_every=0)
+        s64.close()
+        cd_err.append(abs(float(h1["cd"][0][i]) - cd64) / abs(cd64))
+        if g64 != 0.0:
+            g_err.append(abs(float(h1["grad"][0][i]) - g64) / abs(g64))
+        else:
+            g_err.append(0.0 if float(h1["grad"][0][i]) == 0.0 else float("inf"))
+    torch.cuda.empty_cache()
     return {"instances": len(inst), "cells": cells, "block": blk, "segment_steps": seg,
+            "cd_rel_err_vs_fp64_max": max(cd_err), "grad_rel_err_vs_fp64_max": max(g_err),
+            "fp64_checked_instances": n_check,
             "recomputed_steps": rec, "workspace_gb": round(wbytes / 1e9, 1),
             "autotune_s": round(t_tune, 2), "graph_capture_s": round(graph_s, 3),
             "graph_kernel_launches": launches, "s_per_iter": round(t, 3),
@@ -354,48 +389,70 @@ def run_ours(args):
     n_cells = NX * NY * NZ
     peak, peak_kind = _peaks()
 
-    # headline: FP32 storage
-    sim = _make_sim("fp32")
+    # clocks and throttle reasons over the whole arm (the headline's timed
+    # region alone is a few ms, shorter than the sampling interval)
     clocks = ClockSampler(local)
     clocks.start()
+
+    # headline: FP32 storage
+    sim = _make_sim("fp32")
     t = _time_steps(sim, args.steps, args.warmup, barrier)
-    clk = clocks.stop()
     t = max_over_ranks(t)
     mlups = aggregate_mlups(ws, n_cells, args.steps, t)
     per_launch = t / args.steps
     achieved = BYTES_PER_UPDATE["fp32"] * n_cells / per_launch / 1e9
 
-    # e2e through the public API with host buffers: chunks of 500 steps, each
-    # H2D of the host state, the steps, D2H of the state and of the sampled Cd
+    # e2e through the public API with host buffers (pinned): each chunk of
+    # 500 steps is set_state_host (one H2D straight into the solver's f
+    # buffer), the steps with the Cd sampled after the last one,
+    # get_state_host (one D2H: the sample pass already left f in the
+    # solver) and the Cd read back -- the reference drivers' sync pattern
+    # (examples/10:93-97).  CUDA events split each chunk into its phases.
     chunk = 500
-    n_chunks = max(1, args.steps // chunk)
+    n_chunks = max(4, args.steps // chunk)
     f_host = sim.equilibrium_state().cpu().pin_memory()
     f_out = torch.empty_like(f_host).pin_memory()
     cd_host = torch.empty((1, 4), dtype=torch.float64).pin_memory()
-    f_dev = torch.empty_like(f_host, device="cuda")
+    samples = torch.zeros((1, 4), dtype=torch.float64, device="cuda")
+    ev = [torch.cuda.Event(enable_timing=True) for _ in range(5)]
+    phase_ms = [0.0, 0.0, 0.0, 0.0]
 
-    def e2e_chunk():
-        f_dev.copy_(f_host, non_blocking=True)
-        sim.set_state(f_dev)
-        s = sim.run(chunk, sample_every=chunk)
-        sim.get_state(out=f_dev)
-        f_out.copy_(f_dev, non_blocking=True)
-        cd_host.copy_(s, non_blocking=True)
+    def e2e_chunk(timed):
+        stream = torch.cuda.current_stream()
+        ev[0].record(stream)
+        sim.set_state_host(f_host)
+        ev[1].record(stream)
+        sim.run(chunk, sample_every=chunk, samples=samples)
+        ev[2].record(stream)
+        sim.get_state_host(f_out)
+        ev[3].record(stream)
+        cd_host.copy_(samples, non_blocking=True)
+        ev[4].record(stream)
         torch.cuda.synchronize()
+        if timed:
+            for k in range(4):
+                phase_ms[k] += ev[k].elapsed_time(ev[k + 1])
 
     # one untimed chunk: the first device access to freshly pinned host pages
-    # costs ~250 ms once (measured 310 ms for the first chunk, 61 ms after)
-    e2e_chunk()
+    # costs ~250 ms once
+    e2e_chunk(False)
     barrier()
     torch.cuda.synchronize()
     t0 = time.perf_counter()
     for _ in range(n_chunks):
-        e2e_chunk()
+        e2e_chunk(True)
     t_e2e = max_over_ranks(time.perf_counter() - t0)
     e2e_mlups = aggregate_mlups(ws, n_cells, chunk * n_chunks, t_e2e)
     state_bytes = 19 * n_cells * 4
     cd_last = float(cd_host[0, 3])
     sim.close()
+    per = [v / n_chunks for v in phase_ms]
+    e2e_note = ("public API (set_state_host, run, get_state_host), pinned host state in/out "
+                "every %d-step chunk, Cd read back; %d timed chunks after one untimed; per chunk "
+                "(CUDA events): H2D %.2f ms, %d steps + final Cd sample pass %.2f ms, D2H %.2f ms, "
+                "Cd read %.3f ms; host wall %.2f ms per chunk"
+                % (chunk, n_chunks, per[0], chunk, per[1], per[2], per[3],
+                   1e3 * t_e2e / n_chunks))
 
     # secondary lines: 16-bit storage of f - f_eq(1, U)
     extra = {}
@@ -440,6 +497,7 @@ def run_ours(args):
                "sample": "%d step(s) of the full 256x128x128 workload on the torch-CPU "
                          "restatement of jax_lbm (%d threads)" % (steps_cpu, threads)}
 
+    clk = clocks.stop()
     if rank == 0:
         line = {
             "metric": "fwd MLUPS at 256x128x128 (MRT+Smagorinsky sphere step)",
@@ -447,9 +505,7 @@ def run_ours(args):
             "warmup": args.warmup, "ms_per_step": round(1e3 * t / args.steps, 5),
             "higher_is_better": True, "scaling": "weak", "vs_baseline": None,
             "dtype": "f32", "data": "synthetic",
-            "config": {"workload": WORKLOAD, "grid": [NX, NY, NZ], "storage": "fp32",
-                       "tau": round(TAU, 6), "l2": "inputs larger than L2 (A/B state 638 MB)",
-                       "parallelism": "replicas" if ws > 1 else "single GPU"},
+            "config": bench_config(ws),
             "roofline": {"bound": "hbm", "achieved": round(achieved, 1), "peak": peak,
                          "unit": "GB/s", "frac": round(achieved / peak, 4),
                          "peak_kind": peak_kind,
@@ -459,8 +515,9 @@ def run_ours(args):
             "e2e": {"value": round(e2e_mlups, 1), "unit": "MLUPS",
                     "h2d_bytes_per_step": state_bytes // chunk,
                     "d2h_bytes_per_step": (state_bytes + 32) // chunk,
-                    "note": "public API, host pinned state in/out every %d-step chunk, Cd read "
-                            "back; one untimed warm-up chunk" % chunk},
+                    "phases_ms_per_chunk": {"h2d": round(per[0], 3), "run": round(per[1], 3),
+                                            "d2h": round(per[2], 3), "cd": round(per[3], 4)},
+                    "note": e2e_note},
             "gpu_launches": args.steps,
             "clocks": clk,
             "storage16": extra,
@@ -471,6 +528,55 @@ def run_ours(args):
         print(json.dumps(line))
     if dist is not None:
         dist.destroy_process_group()
+    return 0
+
+
+def run_profile_case(spec):
+    """A small fixed workload for ncu captures of one kernel family (no
+    timing, no JSON line):
+
+      NXxNYxNZ:STORAGE:STEPS[:grad]  the bench step (MRT + Smagorinsky Cs 0.1,
+          pre-collision guard, dist-mask Bouzidi sphere r = 0.5 world at the
+          domain centre, Re 100 on D = nx/8) for STEPS steps; with ``grad`` one
+          dCd/dr evaluation over STEPS steps instead (guard off, segment
+          STEPS/4: forward, recompute and adjoint kernels);
+      batch:COUNT:STEPS  one batched gradient evaluation (no graph) of the
+          first COUNT instances of the batched workload, segment STEPS/2.
+    """
+    import torch
+    parts = spec.split(":")
+    if parts[0] == "batch":
+        from lbm_jax_autodiff_gb300.batch import Batch, config5_instances
+        count = int(parts[1]) if len(parts) > 1 else 16
+        steps = int(parts[2]) if len(parts) > 2 else 8
+        inst, sph = config5_instances(count)
+        b = Batch(inst)
+        b.set_spheres(sph)
+        b.set_equilibrium()
+        cd, g = b.cd_and_grad(steps, checkpoint_every=max(1, steps // 2), use_graph=False)
+        torch.cuda.synchronize()
+        print("profile case ok: cells", b.cells, "cd[:2]", cd[:2], "g[:2]", g[:2])
+        b.close()
+        return 0
+    from lbm_jax_autodiff_gb300 import Simulation
+    nx, ny, nz = [int(v) for v in parts[0].split("x")]
+    storage = parts[1] if len(parts) > 1 else "fp32"
+    steps = int(parts[2]) if len(parts) > 2 else 8
+    grad = len(parts) > 3 and parts[3] == "grad"
+    tau = 3 * U * (nx / 8.0) / RE + 0.5
+    sim = Simulation(nx, ny, nz, tau, collision="mrt", storage=storage, use_smagorinsky=True,
+                     smagorinsky_cs=CS, guard="off" if grad else "pre",
+                     inlet_velocity=(U, 0.0, 0.0))
+    sim.set_sphere(0.5, kind="dist", q_mode="bouzidi", porosity="hard")
+    sim.set_state(sim.equilibrium_state())
+    if grad:
+        cd, g = sim.cd_and_grad(steps, checkpoint_every=max(1, steps // 4))
+        print("cd", cd, "dcd_dr", g)
+    else:
+        sim.run(steps)
+    torch.cuda.synchronize()
+    print("profile case ok: links", sim.link_count)
+    sim.close()
     return 0
 
 
@@ -486,7 +592,12 @@ def main():
     ap.add_argument("--grad-steps", type=int, default=2000)
     ap.add_argument("--grad-reps", type=int, default=2)
     ap.add_argument("--no-batch", action="store_true", help="skip the batched-instances line")
+    ap.add_argument("--profile-case", default=None,
+                    help="run a small fixed workload for an ncu capture instead of the bench "
+                         "(NXxNYxNZ:STORAGE:STEPS[:grad] or batch:COUNT:STEPS)")
     args = ap.parse_args()
+    if args.profile_case:
+        return run_profile_case(args.profile_case)
     if args.warmup < 3:
         args.warmup = 3
     if args.impl == "reference":

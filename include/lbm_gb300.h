@@ -113,6 +113,15 @@ int lbm_set_inlet_profile(lbm_sim* sim, const void* u_face, void* stream);
  * set: the state after 0 steps; get: the reference's f after the steps run so far. */
 int lbm_set_state(lbm_sim* sim, const void* f, void* stream);
 int lbm_get_state(lbm_sim* sim, void* f, void* stream);
+/* The same with f in host memory (pinned for an asynchronous copy): one
+ * cudaMemcpyAsync straight between the host buffer and the handle's own f
+ * buffer, no device staging by the caller.  get: when the last lbm_run call
+ * sampled its final step, that sample pass already left f in the handle and
+ * the copy is all that runs; otherwise one stream-only pass writes it first.
+ * For drivers that keep the state on the host between chunks of steps, as
+ * the reference's examples do every sampling interval (examples/10:93-97). */
+int lbm_set_state_host(lbm_sim* sim, const void* f_host, void* stream);
+int lbm_get_state_host(lbm_sim* sim, void* f_host, void* stream);
 
 /* Advance n_steps.  If sample_every > 0, after every sample_every-th step of
  * this call the momentum-exchange force and Cd are written to
@@ -143,6 +152,15 @@ int lbm_get_adjoint_plan(lbm_sim* sim, int* segment_steps, int* recomputed_steps
                          unsigned long long* workspace_bytes);
 /* Free the adjoint population workspace. */
 int lbm_release_workspace(lbm_sim* sim);
+/* Cap, in bytes, on the population workspace (checkpoints + stash) that the
+ * automatic plan (checkpoint_every <= 0) may take; 0 (the default) lets it
+ * use the free device memory minus a reserve of 2 GiB + 2 % of the device.
+ * For a library sharing the device with a framework that holds a memory
+ * pool (JAX preallocates 75 % of the device, torch caches freed blocks).
+ * A cap below the smallest workspace, ceil(N/K) - 1 + K states at
+ * K ~ sqrt(N), makes lbm_cd_and_grad fail with LBM_ERR_NOMEM.  Counterpart
+ * of jax.checkpoint's memory/recompute trade-off (examples/08:49-66). */
+int lbm_set_workspace_limit(lbm_sim* sim, unsigned long long max_bytes);
 
 /* Host-side queries (synchronise `stream`). */
 int lbm_get_projected_area(lbm_sim* sim, double* area_host);
@@ -256,8 +274,10 @@ int lbm_momentum_exchange_vjp(int dtype, const void* q, const double* g_force, v
  * library, which every GPU that loads the library keeps until exit.
  *  - Grids of at most 16,777,216 cells; larger ones return LBM_ERR_UNSUPPORTED.
  *  - The first call on a device looks up that array's device address
- *    (cudaGetSymbolAddress, with that device current); make that first call
- *    before any stream capture.
+ *    (cudaGetSymbolAddress, with that device current), and so does the first
+ *    call after the device's context was torn down and created again (e.g.
+ *    cudaDeviceReset), which moves the array; make such a first call before
+ *    any stream capture.
  *  - All calls on a device share the array: calls that overlap on the GPU
  *    (concurrent streams or threads) race and must be serialised.  Each call
  *    writes every partial it reads, so nothing needs clearing in between. */
@@ -373,6 +393,10 @@ int lbm_batch_autotune(lbm_batch* batch, int probe_steps, int n_steps, int* bloc
                        int* checkpoint_out, void* stream);
 int lbm_batch_get_plan(lbm_batch* batch, int* block, int* segment_steps, int* recomputed_steps,
                        unsigned long long* workspace_bytes, double* graph_build_seconds);
+/* Cap, in bytes, on the population workspace of all instances together
+ * under the automatic plan (checkpoint_every 0, lbm_batch_autotune); 0 = no
+ * cap.  As lbm_set_workspace_limit. */
+int lbm_batch_set_workspace_limit(lbm_batch* batch, unsigned long long max_bytes);
 /* Kernel launches (graph nodes) of the last captured gradient evaluation
  * (0 before the first capture). */
 int lbm_batch_graph_launches(lbm_batch* batch, long long* launches);

@@ -108,6 +108,8 @@ SIGNATURES = {
     "lbm_set_inlet_profile": [_vp, _vp, _vp],
     "lbm_set_state": [_vp, _vp, _vp],
     "lbm_get_state": [_vp, _vp, _vp],
+    "lbm_set_state_host": [_vp, _vp, _vp],
+    "lbm_get_state_host": [_vp, _vp, _vp],
     "lbm_run": [_vp, _i, _i, _vp, _vp],
     "lbm_cd_and_grad": [_vp, _i, _i, ctypes.POINTER(_d), ctypes.POINTER(_d), _vp, _vp, _vp],
     "lbm_get_projected_area": [_vp, ctypes.POINTER(_d)],
@@ -117,6 +119,7 @@ SIGNATURES = {
     "lbm_get_adjoint_plan": [_vp, ctypes.POINTER(_i), ctypes.POINTER(_i),
                              ctypes.POINTER(ctypes.c_ulonglong)],
     "lbm_release_workspace": [_vp],
+    "lbm_set_workspace_limit": [_vp, ctypes.c_ulonglong],
     # geometry builders
     "lbm_sphere_fields": [_i, _i, _i, _i, ctypes.POINTER(LBMSphereC), _vp, _vp, _vp, _vp, _vp],
     "lbm_box_fields": [_i, _i, _i, _i, ctypes.POINTER(_d), ctypes.POINTER(_d), _vp, _vp, _vp],
@@ -166,6 +169,7 @@ SIGNATURES = {
     "lbm_batch_get_plan": [_vp, ctypes.POINTER(_i), ctypes.POINTER(_i), ctypes.POINTER(_i),
                            ctypes.POINTER(ctypes.c_ulonglong), ctypes.POINTER(_d)],
     "lbm_batch_graph_launches": [_vp, ctypes.POINTER(ctypes.c_longlong)],
+    "lbm_batch_set_workspace_limit": [_vp, ctypes.c_ulonglong],
 }
 _RESTYPES = {"lbm_status_string": ctypes.c_char_p, "lbm_last_error": ctypes.c_char_p}
 

@@ -139,6 +139,11 @@ class Batch:
         return out
 
     # -- tuning -------------------------------------------------------------
+    def set_workspace_limit(self, max_bytes):
+        """Cap the population workspace of all instances under the automatic
+        plan (checkpoint_every=0, autotune); 0 removes the cap."""
+        nat.call("lbm_batch_set_workspace_limit", self._h, int(max_bytes))
+
     def set_block(self, block):
         nat.call("lbm_batch_set_block", self._h, int(block))
 

@@ -98,6 +98,7 @@ struct lbm_batch {
   // gradient plan
   int plan_K = 0, plan_recompute = 0;
   unsigned long long plan_bytes = 0;
+  size_t workspace_limit = 0;   // cap on the automatic plan's workspace, all instances (0: none)
   // captured gradient evaluation
   cudaStream_t gs = nullptr;
   cudaEvent_t ev_in = nullptr, ev_out = nullptr;
@@ -266,13 +267,13 @@ int plan_workspace(lbm_batch* b, int N, int K) {
     LBM_TRY(cuda_check(cudaMemGetInfo(&free_b, &total_b), "cudaMemGetInfo"));
     free_b += have;
     const size_t reserve = (size_t(2) << 30) + total_b / 50;
-    const long long M = free_b > reserve ? (long long)((free_b - reserve) / per_state) : 0;
-    K = N;
-    while (K > 1 && (long long)((N + K - 1) / K) + K > M) --K;
+    size_t avail = free_b > reserve ? free_b - reserve : 0;
+    if (b->workspace_limit && b->workspace_limit < avail) avail = b->workspace_limit;
+    LBM_TRY(plan_segment(N, (long long)(avail / per_state), per_state, &K));
   }
   if (K > N) K = N;
   const int nseg = (N + K - 1) / K;
-  const size_t need = size_t(nseg - 1) + size_t(K + 1);
+  const size_t need = size_t(nseg - 1) + size_t(K);
   for (auto* s : b->sims) {
     if (s->states_cap < need) {
       cudaFree(s->states);
@@ -302,7 +303,7 @@ int step_b(lbm_batch* b, int src, int dst, int extra, cudaStream_t st) {
 int enqueue_grad(lbm_batch* b, int N, int K, const AdamP* adam, cudaStream_t st) {
   const int nseg = (N + K - 1) / K;
   auto ckpt = [&](int c) { return c; };
-  auto stash = [&](int j) { return nseg - 1 + j; };
+  auto stash = [&](int j) { return nseg - 2 + j; };   // j = 1..K
   auto seg_a = [&](int c) -> int {
     if (c <= 0) return 0;
     if (c >= nseg) return N;
@@ -552,6 +553,7 @@ int lbm_batch_set_equilibrium(lbm_batch* b, void* stream) {
     LBM_TRY(cuda_check(cudaGetLastError(), "fill"));
     s->state_is_S = 0;
     s->steps = 0;
+    s->fbuf_step = 0;
   }
   b->state_is_S = 0;
   b->steps = 0;
@@ -610,6 +612,7 @@ int lbm_batched_run(lbm_batch* b, int n_steps, int sample_every, double* samples
     s->state_is_S = b->state_is_S;
     s->cur = b->cur;
     s->steps = b->steps;
+    if (si >= 0) s->fbuf_step = b->steps;   // the last sample pass wrote f into f_0's buffer
   }
   return LBM_OK;
 }
@@ -759,6 +762,12 @@ int lbm_batch_get_plan(lbm_batch* b, int* block, int* segment_steps, int* recomp
   *recomputed_steps = b->plan_recompute;
   *workspace_bytes = b->plan_bytes;
   *graph_build_seconds = b->graph_seconds;
+  return LBM_OK;
+}
+
+int lbm_batch_set_workspace_limit(lbm_batch* b, unsigned long long max_bytes) {
+  if (!b) return set_error(LBM_ERR_ARG, "lbm_batch_set_workspace_limit: null handle");
+  b->workspace_limit = size_t(max_bytes);
   return LBM_OK;
 }
 

@@ -453,7 +453,35 @@ int lbm_set_state(lbm_sim* s, const void* f, void* stream) {
                      "state copy"));
   s->state_is_S = 0;
   s->steps = 0;
+  s->fbuf_step = 0;
   return LBM_OK;
+}
+
+int lbm_set_state_host(lbm_sim* s, const void* f_host, void* stream) {
+  if (!s || !f_host) return set_error(LBM_ERR_ARG, "lbm_set_state_host: null argument");
+  cudaStream_t st = static_cast<cudaStream_t>(stream);
+  LBM_TRY(cuda_check(cudaMemcpyAsync(s->fbuf, f_host, s->n * Q * s->re_bytes,
+                                     cudaMemcpyHostToDevice, st),
+                     "state H2D"));
+  s->state_is_S = 0;
+  s->steps = 0;
+  s->fbuf_step = 0;
+  return LBM_OK;
+}
+
+int lbm_get_state_host(lbm_sim* s, void* f_host, void* stream) {
+  if (!s || !f_host) return set_error(LBM_ERR_ARG, "lbm_get_state_host: null argument");
+  cudaStream_t st = static_cast<cudaStream_t>(stream);
+  if (s->state_is_S && s->fbuf_step != s->steps) {
+    // f of the current step is not in fbuf yet: one stream-only pass (the
+    // first-step input f_0 it overwrites is no longer needed)
+    if (!s->have_geometry) return set_error(LBM_ERR_STATE, "lbm_get_state_host: no geometry");
+    LBM_TRY(launch(s, s->S[s->cur], s->fbuf, SF_STREAM_ONLY, st));
+    s->fbuf_step = s->steps;
+  }
+  return cuda_check(cudaMemcpyAsync(f_host, s->fbuf, s->n * Q * s->re_bytes,
+                                    cudaMemcpyDeviceToHost, st),
+                    "state D2H");
 }
 
 int lbm_get_state(lbm_sim* s, void* f, void* stream) {
@@ -502,8 +530,10 @@ int lbm_run(lbm_sim* s, int n_steps, int sample_every, double* samples, void* st
   }
   const long long si = want_sample(s->steps, k0);
   if (si >= 0) {
-    // sample after the last step: stream-only pass with the force, state unchanged
+    // sample after the last step: stream-only pass with the force, state
+    // unchanged; fbuf then holds the reference f of this step
     LBM_TRY(launch(s, s->S[s->cur], s->fbuf, SF_STREAM_ONLY | SF_FORCE, st));
+    s->fbuf_step = s->steps;
     LBM_TRY(cuda_check(launch_force_finalize(s->partials, s->nblocks, da, samples + 4 * si, st),
                        "force finalize"));
   }
@@ -542,20 +572,21 @@ int lbm_cd_and_grad(lbm_sim* s, int n_steps, int checkpoint_every, double* cd_ho
   }
   // Segment length K: the last segment's populations come straight from the
   // forward pass, earlier segments are recomputed from their checkpoints, so
-  // N - K steps are recomputed and ceil(N/K) - 1 + K + 1 states are stored.
+  // N - K steps are recomputed and ceil(N/K) - 1 + K states are stored
+  // (a checkpoint per segment start after the first, K stashed states).
   int K = checkpoint_every;
   if (K <= 0) {
     size_t free_b = 0, total_b = 0;
     LBM_TRY(cuda_check(cudaMemGetInfo(&free_b, &total_b), "cudaMemGetInfo"));
     free_b += s->states_cap * state_bytes;   // the current workspace is reusable
     const size_t reserve = (size_t(2) << 30) + total_b / 50;
-    const long long M = free_b > reserve ? (long long)((free_b - reserve) / state_bytes) : 0;
-    K = N;
-    while (K > 1 && (long long)((N + K - 1) / K) + K > M) --K;
+    size_t avail = free_b > reserve ? free_b - reserve : 0;
+    if (s->workspace_limit && s->workspace_limit < avail) avail = s->workspace_limit;
+    LBM_TRY(plan_segment(N, (long long)(avail / state_bytes), state_bytes, &K));
   }
   if (K > N) K = N;
   const int nseg = (N + K - 1) / K;
-  const size_t need = size_t(nseg - 1) + size_t(K + 1);
+  const size_t need = size_t(nseg - 1) + size_t(K);
   if (s->states_cap < need) {
     cudaFree(s->states);
     s->states = nullptr;
@@ -568,7 +599,8 @@ int lbm_cd_and_grad(lbm_sim* s, int n_steps, int checkpoint_every, double* cd_ho
   s->plan_bytes = need * state_bytes;
   char* base = static_cast<char*>(s->states);
   auto ckpt = [&](int c) -> void* { return base + size_t(c) * state_bytes; };  // S_{a_{c+1}-1}
-  auto stash = [&](int j) -> void* { return base + size_t(nseg - 1 + j) * state_bytes; };
+  // stash(j), j = 1..K: S_{a+j-1} of the segment [a, a+K) being run backwards
+  auto stash = [&](int j) -> void* { return base + size_t(nseg - 2 + j) * state_bytes; };
   // segment c covers [seg_a(c), seg_a(c+1)); the last one has exactly K steps
   auto seg_a = [&](int c) -> int {
     if (c <= 0) return 0;
@@ -733,6 +765,12 @@ int lbm_get_adjoint_plan(lbm_sim* s, int* segment_steps, int* recomputed_steps,
   *segment_steps = s->plan_K;
   *recomputed_steps = s->plan_recompute;
   *workspace_bytes = (unsigned long long)s->plan_bytes;
+  return LBM_OK;
+}
+
+int lbm_set_workspace_limit(lbm_sim* s, unsigned long long max_bytes) {
+  if (!s) return set_error(LBM_ERR_ARG, "lbm_set_workspace_limit: null handle");
+  s->workspace_limit = size_t(max_bytes);
   return LBM_OK;
 }
 

@@ -13,6 +13,8 @@
 // fixed array compiled into this library (kNoAllocMaxBlocks x 3 doubles,
 // 1.5 MiB).  Every GPU that loads the library holds that array until the
 // process exits.
+#include <cuda.h>   // CUcontext / CUresult types; the driver calls go through
+                    // cudaGetDriverEntryPointByVersion, so no -lcuda is needed
 #include <mutex>
 
 #include "../../include/lbm_gb300.h"
@@ -32,23 +34,71 @@ constexpr int kMaxDevices = 64;
 // them, so nothing needs clearing between calls.
 static __device__ __align__(256) double g_force_scratch[kNoAllocMaxBlocks * 3];
 
+// Device address of g_force_scratch per device, with the id of the CUDA
+// context it was looked up in.  A module's globals live in a context: after
+// cudaDeviceReset (or any teardown and re-creation of the primary context)
+// the library's module is loaded again at a new address, so an address
+// cached under the old context id is looked up again instead of reused.
+struct ScratchSlot {
+  unsigned long long ctx_id;
+  double* addr;
+};
 std::mutex g_scratch_mu;
-double* g_scratch_addr[kMaxDevices] = {};
+ScratchSlot g_scratch[kMaxDevices] = {};
+
+using CtxGetCurrentFn = CUresult (*)(CUcontext*);
+using CtxGetIdFn = CUresult (*)(CUcontext, unsigned long long*);
+
+// Id of the calling thread's current context (cuCtxGetId: unique over the
+// life of the process), 0 when no context is current yet.
+int current_context_id(unsigned long long* id) {
+  static CtxGetCurrentFn get_current = nullptr;
+  static CtxGetIdFn get_id = nullptr;
+  static int resolved = 0;   // guarded by g_scratch_mu
+  *id = 0;
+  if (!resolved) {
+    cudaDriverEntryPointQueryResult q1 = cudaDriverEntryPointSymbolNotFound, q2 = q1;
+    LBM_TRY(cuda_check(cudaGetDriverEntryPointByVersion("cuCtxGetCurrent", (void**)&get_current,
+                                                        12000, cudaEnableDefault, &q1),
+                       "cudaGetDriverEntryPointByVersion(cuCtxGetCurrent)"));
+    LBM_TRY(cuda_check(cudaGetDriverEntryPointByVersion("cuCtxGetId", (void**)&get_id, 12000,
+                                                        cudaEnableDefault, &q2),
+                       "cudaGetDriverEntryPointByVersion(cuCtxGetId)"));
+    if (q1 != cudaDriverEntryPointSuccess || q2 != cudaDriverEntryPointSuccess || !get_current ||
+        !get_id)
+      return set_error(LBM_ERR_CUDA, "lbm_momentum_exchange_noalloc: driver lacks cuCtxGetId");
+    resolved = 1;
+  }
+  CUcontext ctx = nullptr;
+  if (get_current(&ctx) != CUDA_SUCCESS)
+    return set_error(LBM_ERR_CUDA, "lbm_momentum_exchange_noalloc: cuCtxGetCurrent failed");
+  if (ctx && get_id(ctx, id) != CUDA_SUCCESS)
+    return set_error(LBM_ERR_CUDA, "lbm_momentum_exchange_noalloc: cuCtxGetId failed");
+  return LBM_OK;
+}
 
 // Device address of g_force_scratch on the current device.  Looked up with
-// cudaGetSymbolAddress the first time each device calls in (that device being
-// current); host code must not use the symbol itself as a device pointer.
+// cudaGetSymbolAddress, with that device current, the first time a device
+// calls in and again whenever the device's context has changed since; host
+// code must not use the symbol itself as a device pointer.
 int scratch_address(double** out) {
   int dev = 0;
   LBM_TRY(cuda_check(cudaGetDevice(&dev), "cudaGetDevice"));
+  if (dev < 0 || dev >= kMaxDevices)
+    return set_error(LBM_ERR_UNSUPPORTED, "lbm_momentum_exchange_noalloc: device ordinal >= 64");
   std::lock_guard<std::mutex> lock(g_scratch_mu);
-  if (dev >= 0 && dev < kMaxDevices && g_scratch_addr[dev]) {
-    *out = g_scratch_addr[dev];
+  unsigned long long id = 0;
+  LBM_TRY(current_context_id(&id));
+  if (id != 0 && g_scratch[dev].addr && g_scratch[dev].ctx_id == id) {
+    *out = g_scratch[dev].addr;
     return LBM_OK;
   }
   void* p = nullptr;
+  // binds the device's primary context to this thread if none was current
   LBM_TRY(cuda_check(cudaGetSymbolAddress(&p, g_force_scratch), "cudaGetSymbolAddress"));
-  if (dev >= 0 && dev < kMaxDevices) g_scratch_addr[dev] = static_cast<double*>(p);
+  if (id == 0) LBM_TRY(current_context_id(&id));
+  g_scratch[dev].ctx_id = id;
+  g_scratch[dev].addr = static_cast<double*>(p);
   *out = static_cast<double*>(p);
   return LBM_OK;
 }

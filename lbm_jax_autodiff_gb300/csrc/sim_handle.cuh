@@ -3,6 +3,7 @@
 // blocks from a handle.
 #pragma once
 
+#include <cstdio>
 #include <cstring>
 
 #include "../../include/lbm_gb300.h"
@@ -88,6 +89,7 @@ struct lbm_sim {
   int state_is_S = 0;        // 0: f_k in fbuf; 1: S_{k-1} in S[cur]
   long long steps = 0;
   void* fbuf = nullptr;      // reference-layout f (compute dtype)
+  long long fbuf_step = -1;  // fbuf holds the reference f after this many steps (-1: none)
   uint32_t* tag = nullptr;
   LinkRec* rec = nullptr;
   int nrec = 0;
@@ -117,7 +119,27 @@ struct lbm_sim {
   int plan_K = 0;            // last adjoint plan: segment length, recomputed steps, bytes
   int plan_recompute = 0;
   size_t plan_bytes = 0;
+  size_t workspace_limit = 0;  // cap on the population workspace of the automatic plan (0: none)
 };
+
+// Longest segment length K in [1, N] whose workspace, ceil(N/K) - 1 + K
+// states, fits in `max_states` states.  The count falls as K falls from N to
+// about sqrt(N) and rises below that, so the search stops there; when even
+// the smallest workspace does not fit, LBM_ERR_NOMEM names the bytes it needs.
+inline int plan_segment(int N, long long max_states, size_t state_bytes, int* K_out) {
+  auto states = [&](long long K) { return (N + K - 1) / K - 1 + K; };
+  long long K = N;
+  while (K > 1 && states(K) > max_states && states(K - 1) <= states(K)) --K;
+  if (states(K) > max_states) {
+    char msg[200];
+    snprintf(msg, sizeof(msg),
+             "adjoint workspace: %d steps need at least %lld states (%.3g GB), %lld fit",
+             N, states(K), double(states(K)) * double(state_bytes) / 1e9, max_states);
+    return set_error(LBM_ERR_NOMEM, msg);
+  }
+  *K_out = int(K);
+  return LBM_OK;
+}
 
 using namespace lbm;
 

@@ -176,6 +176,27 @@ class Simulation:
         _require_cuda(f, "f", self.dtype, 19 * self.n)
         nat.call("lbm_set_state", self._h, _ptr(f), _stream())
 
+    def set_state_host(self, f):
+        """set_state from a host (CPU) tensor, pinned for an asynchronous
+        copy: one host-to-device copy into the solver's own buffer."""
+        if not (torch.is_tensor(f) and not f.is_cuda and f.is_contiguous()):
+            raise TypeError("f must be a contiguous CPU tensor")
+        if f.dtype != self.dtype or f.numel() != 19 * self.n:
+            raise ValueError("f must be a %s tensor of %d elements" % (self.dtype, 19 * self.n))
+        self._keep["f_host_in"] = f
+        nat.call("lbm_set_state_host", self._h, _ptr(f), _stream())
+
+    def get_state_host(self, out):
+        """The reference f after the steps run so far, into a host (CPU)
+        tensor (pinned for an asynchronous copy); asynchronous on the current
+        stream -- synchronise before reading ``out``."""
+        if not (torch.is_tensor(out) and not out.is_cuda and out.is_contiguous()):
+            raise TypeError("out must be a contiguous CPU tensor")
+        if out.dtype != self.dtype or out.numel() != 19 * self.n:
+            raise ValueError("out must be a %s tensor of %d elements" % (self.dtype, 19 * self.n))
+        nat.call("lbm_get_state_host", self._h, _ptr(out), _stream())
+        return out
+
     def get_state(self, out=None):
         if out is None:
             out = torch.empty((19,) + self.shape, dtype=self.dtype, device="cuda")
@@ -241,6 +262,13 @@ class Simulation:
 
     def release_workspace(self):
         nat.call("lbm_release_workspace", self._h)
+
+    def set_workspace_limit(self, max_bytes):
+        """Cap the adjoint population workspace that cd_and_grad's automatic
+        plan (checkpoint_every=0) may take; 0 removes the cap (free device
+        memory minus a reserve).  Use it beside a framework that holds a
+        memory pool."""
+        nat.call("lbm_set_workspace_limit", self._h, int(max_bytes))
 
     # -- queries ------------------------------------------------------------
     @property

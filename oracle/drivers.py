@@ -134,12 +134,20 @@ def cd_of_radius_bgk_f64(radius, nx=32, ny=16, nz=16, n_steps=10, u_inlet=0.05,
 def simulate_cd(radius, nx, ny, nz, n_steps, tau, u_inlet=0.05, q_mode="bouzidi",
                 porosity_mode="soft", sharpness=20.0, collision="mrt", smagorinsky_cs=None,
                 periodic_yz=True, center=(0.0, 0.0, 0.0), dtype=torch.float32,
-                disc_floor=1e-10, a_eps=1e-20, q_leaf=None, consts=None, return_parts=False):
+                disc_floor=1e-10, a_eps=1e-20, q_leaf=None, consts=None, return_parts=False,
+                remat_chunk=None):
     """The reference gradient drivers' simulate_cd (examples/11:139-165,
     examples/08:69-93): build the four-mode sphere from ``radius`` (a tensor
     that may require grad), run n_steps of collide -> porosity blend ->
     stream -> Zou-He, and return Cd from the final step.  ``q_leaf`` replaces
-    the q buffer (to differentiate with respect to q directly)."""
+    the q buffer (to differentiate with respect to q directly).
+
+    ``remat_chunk`` = K runs the steps in chunks of K under
+    torch.utils.checkpoint, so autograd keeps one state per chunk and
+    recomputes a chunk's steps in the backward pass -- the
+    ``jax.checkpoint`` chunking of the reference drivers (examples/08:49-66,
+    examples/12:_chunked_scan).  The gradient is the same; only the memory
+    of a long run at a large grid changes."""
     from .geometry import sphere_geometry
     c = consts or ops.consts_for(dtype)
     por, solid, q = sphere_geometry(nx, ny, nz, radius, q_mode, porosity_mode, sharpness, center,
@@ -149,7 +157,21 @@ def simulate_cd(radius, nx, ny, nz, n_steps, tau, u_inlet=0.05, q_mode="bouzidi"
     f = initial_state(nx, ny, nz, u_inlet, dtype, c)
     cfg = StepConfig(tau=tau, inlet=(u_inlet, 0.0, 0.0), collision=collision,
                      smagorinsky_cs=smagorinsky_cs, periodic_yz=periodic_yz)
-    f, f_post, _ = run(f, q, cfg, n_steps, porosity=por, consts=c)
+    if remat_chunk:
+        from torch.utils.checkpoint import checkpoint
+
+        def chunk(f_in, fp_in, q_in, p_in, k):
+            f_out, fp_out, _ = run(f_in, q_in, cfg, k, porosity=p_in, consts=c)
+            return f_out, fp_out
+
+        f_post = f
+        done = 0
+        while done < n_steps:
+            k = min(int(remat_chunk), n_steps - done)
+            f, f_post = checkpoint(chunk, f, f_post, q, por, k, use_reentrant=False)
+            done += k
+    else:
+        f, f_post, _ = run(f, q, cfg, n_steps, porosity=por, consts=c)
     area = max(ops.projected_area(solid), 1.0)
     cd, _ = cd_from(f_post, f, q, u_inlet, area)
     if return_parts:

@@ -136,6 +136,30 @@ def modes():
         _save_json("modes_96x48x48.json", out)
 
 
+def config3():
+    """dCd/dr at the config-3 grid: 96x48x48, MRT, Bouzidi ray-sphere q(r),
+    r = 0.5 world (6 cells) centred at cell (24, 24, 24) = world (-2, 0, 0),
+    Re 100 (nu 0.006, tau 0.518); FP64 autograd through the oracle (the
+    jax.grad stand-in) over a 100-step window, for the hard sphere and the
+    sigmoid-soft sphere (alpha 20).  Rematerialised in chunks of 10 steps."""
+    nx, ny, nz, n = 96, 48, 48, 100
+    tau = 3.0 * 0.006 + 0.5
+    dt = torch.float64
+    out = {"grid": [nx, ny, nz], "steps": n, "tau": tau, "center": [-2.0, 0.0, 0.0],
+           "radius": 0.5}
+    torch.set_num_threads(os.cpu_count() or 1)
+    for name, kw in (("hard", dict(q_mode="bouzidi", porosity_mode="hard")),
+                     ("soft20", dict(q_mode="bouzidi", porosity_mode="soft", sharpness=20.0))):
+        r = torch.tensor(0.5, dtype=dt, requires_grad=True)
+        t0 = time.time()
+        cd = drivers.simulate_cd(r, nx, ny, nz, n, tau, center=(-2.0, 0.0, 0.0), dtype=dt,
+                                 consts=consts_for(dt), remat_chunk=10, **kw)
+        cd.backward()
+        out[name] = {"cd": float(cd.detach()), "dcd_dr": float(r.grad), "seconds": time.time() - t0,
+                     "porosity": kw["porosity_mode"], "sharpness": kw.get("sharpness")}
+        _save_json("config3_grad_96x48x48.json", out)
+
+
 if __name__ == "__main__":
     for name in sys.argv[1:] or ["pins", "channel", "sphere", "sphere_periodic", "modes"]:
         globals()[name]()

@@ -283,3 +283,32 @@ def test_full_size_precision_bars(cuda):
     assert abs(g16 - g64) <= 1e-3 * abs(g64), (g16, g64)
     assert abs(cd32 - cd64) <= 1e-4 * abs(cd64), (cd32, cd64)
     assert abs(g32 - g64) <= 1e-5 * abs(g64), (g32, g64)
+
+
+def test_workspace_limit_caps_the_automatic_plan(cuda):
+    """A cap on the adjoint workspace: the automatic plan stays under it and
+    gives the same result as the uncapped plan; a cap below the smallest
+    workspace (ceil(N/K) - 1 + K states at K ~ sqrt(N)) is refused."""
+    from lbm_jax_autodiff_gb300._native import LBMError
+    nx, ny, nz, n = 32, 16, 16, 64
+    sim = _sim(nx, ny, nz, 0.56, storage="fp32")
+    sim.set_sphere(0.5, kind="sigmoid", q_mode="bouzidi", porosity="soft")
+    sim.set_state(sim.equilibrium_state())
+    free = sim.cd_and_grad(n, checkpoint_every=0)
+    K0, rec0, bytes0 = sim.adjoint_plan
+    assert (K0, rec0) == (n, 0)
+    state = 19 * nx * ny * nz * 4
+    assert bytes0 == n * state                        # K stashed states, no checkpoint
+    sim.release_workspace()
+    sim.set_workspace_limit(20 * state)
+    capped = sim.cd_and_grad(n, checkpoint_every=0)
+    K, rec, wbytes = sim.adjoint_plan
+    assert wbytes <= 20 * state and ((n + K - 1) // K - 1 + K) * state == wbytes
+    assert rec == n - K and K < n
+    assert capped == free                             # recomputation is exact
+    sim.set_workspace_limit(14 * state)               # min over K of ceil(64/K) - 1 + K is 15
+    with pytest.raises(LBMError, match="NOMEM"):
+        sim.cd_and_grad(n, checkpoint_every=0)
+    sim.set_workspace_limit(0)
+    assert sim.cd_and_grad(n, checkpoint_every=0) == free
+    sim.close()

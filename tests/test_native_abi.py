@@ -100,3 +100,11 @@ def test_batch_entry_points_reject_null_handles(lib):
     w, g = ctypes.c_ulonglong(), ctypes.c_double()
     assert L.lbm_batch_get_plan(None, ctypes.byref(b), ctypes.byref(k), ctypes.byref(r),
                                 ctypes.byref(w), ctypes.byref(g)) == nat.LBM_ERR_ARG
+
+
+def test_workspace_limits_reject_null_handles(lib):
+    from lbm_jax_autodiff_gb300 import _native as nat
+    L = nat.load()
+    assert L.lbm_set_workspace_limit(None, 1 << 30) == nat.LBM_ERR_ARG
+    assert L.lbm_batch_set_workspace_limit(None, 1 << 30) == nat.LBM_ERR_ARG
+    assert b"null handle" in L.lbm_last_error()

@@ -46,3 +46,24 @@ def test_xla_stream_bgk_inlet_momentum(cuda):
     fr, qr = f.clone().requires_grad_(True), q.clone().requires_grad_(True)
     (L.stream(fr, qr, True) * g).sum().backward()
     assert torch.allclose(gf, fr.grad) and torch.allclose(gq, qr.grad)
+
+
+def test_xla_failure_fills_results_with_nan(cuda):
+    """A target whose call fails writes NaN into its results instead of
+    leaving them unwritten (the legacy custom-call API has no status)."""
+    nx, ny, nz = 12, 6, 6
+    q = -torch.ones((19, nx, ny, nz), dtype=torch.float64, device="cuda")
+    out = torch.zeros((19, nx, ny, nz), dtype=torch.float64, device="cuda")
+    desc = jax_ffi.descriptor(nx, ny, nz, 1, periodic_yz=1)
+    arr = (ctypes.c_void_p * 3)(None, q.data_ptr(), out.data_ptr())   # f missing: LBM_ERR_ARG
+    d = desc.encode()
+    jax_ffi.xla_target("stream")(ctypes.c_void_p(torch.cuda.current_stream().cuda_stream), arr,
+                                 d, len(d))
+    torch.cuda.synchronize()
+    assert torch.isnan(out).all()
+    force = torch.zeros(3, dtype=torch.float64, device="cuda")
+    arr = (ctypes.c_void_p * 4)(q.data_ptr(), None, q.data_ptr(), force.data_ptr())
+    jax_ffi.xla_target("momentum_exchange")(
+        ctypes.c_void_p(torch.cuda.current_stream().cuda_stream), arr, d, len(d))
+    torch.cuda.synchronize()
+    assert torch.isnan(force).all()
