@@ -287,6 +287,57 @@ def _grad_rate(storage, n_steps, reps, barrier, max_over_ranks, peak, ws):
             "achieved_gbs": round(achieved, 1), "frac": round(achieved / peak, 4)}
 
 
+def _cd_time_average(storage, n_steps, smagorinsky, sample_every=500, tail_fraction=0.3):
+    """Cd sampled every `sample_every` steps over n_steps of the sphere at
+    256x128x128 (D = 32, Re 100, pre-collision guard), averaged over the last
+    30 % of the samples as examples/10_cd_convergence.py:88-106 does
+    (n_tail = max(3, int(0.3 n_samples)), mean and population std)."""
+    import torch
+    from lbm_jax_autodiff_gb300 import Simulation
+    sim = Simulation(NX, NY, NZ, TAU, collision="mrt", storage=storage,
+                     use_smagorinsky=smagorinsky, smagorinsky_cs=CS, periodic_yz=True,
+                     guard="pre", inlet_velocity=(U, 0.0, 0.0))
+    sim.set_sphere(0.5, center=(0.0, 0.0, 0.0), kind="dist", q_mode="bouzidi", porosity="hard")
+    sim.set_state(sim.equilibrium_state())
+    t0 = time.perf_counter()
+    smp = sim.run(n_steps, sample_every=sample_every)
+    torch.cuda.synchronize()
+    dt = time.perf_counter() - t0
+    resets = sim.guard_resets
+    sim.close()
+    cd = smp[:, 3].double().cpu()
+    n_tail = max(3, int(cd.numel() * tail_fraction))
+    tail = cd[-n_tail:]
+    return {"cd_mean": float(tail.mean()), "cd_std": float(tail.std(unbiased=False)),
+            "cd_last": float(cd[-1]), "samples": int(cd.numel()), "tail_samples": n_tail,
+            "seconds": round(dt, 2), "guard_resets": int(resets)}
+
+
+def _precision_28k(n_steps):
+    """Config-4 precision form: the 256x128x128 sphere over n_steps (28,000),
+    time-averaged Cd in FP32, FP16, BF16 and FP64 storage with Smagorinsky
+    Cs 0.1, each against FP64; and the examples/10 run (MRT without
+    Smagorinsky) in FP32 and FP16 against the published A100 result
+    1.1854 +/- 0.0705 (paper/make_convergence_figures.py:53-54)."""
+    out = {"steps": n_steps, "sample_every": 500}
+    smag = {}
+    for storage in ("fp64", "fp32", "fp16", "bf16"):
+        smag[storage] = _cd_time_average(storage, n_steps, True)
+    ref = smag["fp64"]["cd_mean"]
+    for storage in ("fp32", "fp16", "bf16"):
+        smag[storage]["cd_mean_rel_err_vs_fp64"] = abs(smag[storage]["cd_mean"] - ref) / abs(ref)
+    out["smagorinsky_cs0.1"] = smag
+    pub_mean, pub_std = 1.1854, 0.0705
+    ex10 = {}
+    for storage in ("fp32", "fp16"):
+        r = _cd_time_average(storage, n_steps, False)
+        r["published_cd_mean"], r["published_cd_std"] = pub_mean, pub_std
+        r["deviation_in_published_std"] = (r["cd_mean"] - pub_mean) / pub_std
+        ex10[storage] = r
+    out["examples10_no_smagorinsky"] = ex10
+    return out
+
+
 def _batch_rate(n_steps, barrier, max_over_ranks):
     """The batched workload: 64 sphere instances (grids 64x32x32 / 96x48x48 /
     128x64x64, radii, q and porosity modes and alpha drawn with seed 0), MRT
@@ -469,7 +520,7 @@ def run_ours(args):
     # shape gradient: dCd/dr evaluations per second over a 2000-step window
     grad = {}
     if not args.no_grad:
-        for storage in ("fp32", "fp16"):
+        for storage in ("fp32", "fp16", "bf16"):
             grad[storage] = _grad_rate(storage, args.grad_steps, args.grad_reps, barrier,
                                        max_over_ranks, peak, ws)
         if grad["fp32"]["evals_per_s"] > 0:
@@ -478,7 +529,7 @@ def run_ours(args):
         # FP64-storage oracle of the same evaluation; errors of every form against it
         ref = _grad_rate("fp64", args.grad_steps, 1, barrier, max_over_ranks, peak, ws)
         grad["fp64"] = ref
-        for storage in ("fp32", "fp16"):
+        for storage in ("fp32", "fp16", "bf16"):
             grad[storage]["cd_rel_err_vs_fp64"] = abs(grad[storage]["cd"] - ref["cd"]) / abs(ref["cd"])
             grad[storage]["grad_rel_err_vs_fp64"] = (abs(grad[storage]["dcd_dr"] - ref["dcd_dr"]) /
                                                      abs(ref["dcd_dr"]))
@@ -486,6 +537,10 @@ def run_ours(args):
     batch = None
     if not args.no_batch:
         batch = _batch_rate(args.grad_steps, barrier, max_over_ranks)
+
+    precision = None
+    if args.cd_steps > 0:
+        precision = _precision_28k(args.cd_steps)
 
     cpu = None
     if rank == 0 and ws == 1 and not args.no_cpu_baseline:
@@ -523,6 +578,7 @@ def run_ours(args):
             "storage16": extra,
             "grad": grad,
             "batch": batch,
+            "precision_28k": precision,
             "cd_last_sample": cd_last,
         }
         print(json.dumps(line))
@@ -592,6 +648,8 @@ def main():
     ap.add_argument("--grad-steps", type=int, default=2000)
     ap.add_argument("--grad-reps", type=int, default=2)
     ap.add_argument("--no-batch", action="store_true", help="skip the batched-instances line")
+    ap.add_argument("--cd-steps", type=int, default=28000,
+                    help="steps of the time-averaged Cd runs of the precision form (0: skip)")
     ap.add_argument("--profile-case", default=None,
                     help="run a small fixed workload for an ncu capture instead of the bench "
                          "(NXxNYxNZ:STORAGE:STEPS[:grad] or batch:COUNT:STEPS)")

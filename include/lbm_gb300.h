@@ -146,6 +146,20 @@ int lbm_run(lbm_sim* sim, int n_steps, int sample_every, double* samples, void* 
 int lbm_cd_and_grad(lbm_sim* sim, int n_steps, int checkpoint_every, double* cd_host,
                     double* dcd_dr_host, void* dcd_dq, void* dcd_df0, void* stream);
 
+/* Vector-Jacobian product of n_steps of lbm_run from the state set by
+ * lbm_set_state: given g_f_final [19][n] (compute dtype), the cotangent of
+ * the reference f after the steps, writes g_f0 [19][n] = its cotangent on
+ * the initial f and, if g_q is not NULL, g_q [19][n] = its cotangent on the
+ * wall distances q of the geometry (zero where there is no link): the
+ * gradient jax.grad takes through simulate (state.py:174-230) with respect
+ * to state.f and state.q.  Forward with checkpoints and recompute as
+ * lbm_cd_and_grad.  Hard-mask geometries only (LBMState has no porosity).
+ * The guard is not differentiated: with a guard on, LBM_ERR_UNSUPPORTED if
+ * it reset any cell in these steps (where no cell is reset the gradient is
+ * that of the unguarded step).  Synchronises `stream`. */
+int lbm_vjp_run(lbm_sim* sim, int n_steps, int checkpoint_every, const void* g_f_final,
+                void* g_f0, void* g_q, void* stream);
+
 /* Plan of the last lbm_cd_and_grad: segment length, recomputed steps and
  * the bytes of the population workspace (checkpoints + stash). */
 int lbm_get_adjoint_plan(lbm_sim* sim, int* segment_steps, int* recomputed_steps,
@@ -329,6 +343,34 @@ void lbm_xla_stream_vjp(void* stream, void** buffers, const char* opaque, size_t
 void lbm_xla_zou_he_inlet_vjp(void* stream, void** buffers, const char* opaque, size_t len);
 void lbm_xla_zou_he_outlet_vjp(void* stream, void** buffers, const char* opaque, size_t len);
 void lbm_xla_momentum_exchange_vjp(void* stream, void** buffers, const char* opaque, size_t len);
+
+/* ---- XLA custom-call targets of the fused solver --------------------------
+ * Same legacy signature; opaque is one lbm_xla_fused_desc (raw bytes).  They
+ * replace a jitted driver's whole loop: lbm_xla_run the lax.scan of
+ * examples/10:69-106 (n_steps with the Cd sampled every sample_every steps),
+ * lbm_xla_cd_and_grad the value_and_grad(simulate_cd) of examples/11:139-176.
+ * The library keeps one solver handle per (device, params) for them, created
+ * on first use and kept until exit; the sphere geometry (radius from the
+ * operand) is rebuilt when it changes, which reads the radius back to the
+ * host (a stream synchronisation).  The last result of each is an int32
+ * status (lbm_status): on failure it is non-zero, the other results are
+ * filled with NaN and the message goes to stderr. */
+typedef struct lbm_xla_fused_desc {
+  lbm_params params;
+  lbm_sphere sphere;      /* its radius is replaced by the radius operand */
+  int32_t n_steps;
+  int32_t sample_every;   /* lbm_xla_run: 0 = no samples (one zero row written) */
+  int32_t checkpoint_every;
+  int32_t pad;
+} lbm_xla_fused_desc;
+
+/* operands: f0 [19][n] (compute dtype), radius f64[1];
+ * results: f [19][n] after n_steps, samples f64[max(1, n_steps / sample_every)][4]
+ * (Fx, Fy, Fz, Cd), status int32[1] */
+void lbm_xla_run(void* stream, void** buffers, const char* opaque, size_t len);
+/* operands: f0 [19][n] (compute dtype), radius f64[1];
+ * results: cd f64[1], dcd_dr f64[1], dcd_dq [19][n] (compute dtype), status int32[1] */
+void lbm_xla_cd_and_grad(void* stream, void** buffers, const char* opaque, size_t len);
 
 /* ---- batched instances --------------------------------------------------
  * Many independent sphere instances -- grids of different sizes, their own

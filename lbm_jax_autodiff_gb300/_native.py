@@ -119,6 +119,7 @@ SIGNATURES = {
     "lbm_get_adjoint_plan": [_vp, ctypes.POINTER(_i), ctypes.POINTER(_i),
                              ctypes.POINTER(ctypes.c_ulonglong)],
     "lbm_release_workspace": [_vp],
+    "lbm_vjp_run": [_vp, _i, _i, _vp, _vp, _vp, _vp],
     "lbm_set_workspace_limit": [_vp, ctypes.c_ulonglong],
     # geometry builders
     "lbm_sphere_fields": [_i, _i, _i, _i, ctypes.POINTER(LBMSphereC), _vp, _vp, _vp, _vp, _vp],

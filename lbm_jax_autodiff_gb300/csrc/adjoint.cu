@@ -566,6 +566,35 @@ __global__ void k_adjoint_seed(StepArgs<Re> a, const double* __restrict__ dj_dfx
   adjoint_seed_cell<Re>(a, dj_dfx, nu, blockIdx.x * blockDim.x + threadIdx.x);
 }
 
+// nu_N = Z^T g for a given cotangent g on the final post-boundary f_N (the
+// reference's state after N steps, state.py:129-171): the Zou-He
+// transposes on the inlet / outlet faces, g itself elsewhere.
+template <class Re>
+__global__ void k_adjoint_seed_dense(StepArgs<Re> a, const Re* __restrict__ gin,
+                                     Re* __restrict__ nu) {
+  const Grid& g = a.g;
+  const int idx = blockIdx.x * blockDim.x + threadIdx.x;
+  if (idx >= g.n) return;
+  const size_t N = size_t(g.n);
+  Re l[Q];
+#pragma unroll
+  for (int i = 0; i < Q; ++i) l[i] = gin[i * N + idx];
+  const int z = idx % g.nz, t = idx / g.nz, y = t % g.ny, x = t / g.ny;
+  if (x == g.nx - 1 && !(a.flags & SF_NO_OUTLET)) zou_he_outlet_T<Re>(l, a.rho_out);
+  if (x == 0 && !(a.flags & SF_NO_INLET)) {
+    Re ux = a.u_in[0], uy = a.u_in[1], uz = a.u_in[2];
+    if (a.flags & SF_INLET_FACE) {
+      const int fi = y * g.nz + z, fn = g.ny * g.nz;
+      ux = a.u_face[fi];
+      uy = a.u_face[fn + fi];
+      uz = a.u_face[2 * fn + fi];
+    }
+    zou_he_inlet_T<Re>(l, ux, uy, uz);
+  }
+#pragma unroll
+  for (int i = 0; i < Q; ++i) nu[i * N + idx] = l[i];
+}
+
 // dJ/dFx = sign(Fx) / (0.5 rho U^2 A + 1e-10) from the finalized force record
 // out = (Fx, Fy, Fz, Cd).
 __global__ void k_dj_dfx(const double* __restrict__ fcd, double dyn_area, double* __restrict__ g) {
@@ -649,6 +678,13 @@ cudaError_t launch_adjoint(const AdjArgs<typename Storage<St>::Re>& A, bool mrt,
 template <class Re>
 cudaError_t launch_adjoint_seed(const StepArgs<Re>& a, const double* dj, Re* nu, cudaStream_t st) {
   k_adjoint_seed<Re><<<nblk(a.g.n), 256, 0, st>>>(a, dj, nu);
+  return cudaGetLastError();
+}
+
+template <class Re>
+cudaError_t launch_adjoint_seed_dense(const StepArgs<Re>& a, const Re* g, Re* nu,
+                                      cudaStream_t st) {
+  k_adjoint_seed_dense<Re><<<nblk(a.g.n), 256, 0, st>>>(a, g, nu);
   return cudaGetLastError();
 }
 
@@ -891,6 +927,10 @@ template cudaError_t launch_adjoint_seed<float>(const StepArgs<float>&, const do
                                                 cudaStream_t);
 template cudaError_t launch_adjoint_seed<double>(const StepArgs<double>&, const double*, double*,
                                                  cudaStream_t);
+template cudaError_t launch_adjoint_seed_dense<float>(const StepArgs<float>&, const float*,
+                                                      float*, cudaStream_t);
+template cudaError_t launch_adjoint_seed_dense<double>(const StepArgs<double>&, const double*,
+                                                       double*, cudaStream_t);
 template cudaError_t launch_scatter_gq<float>(const Grid&, const uint32_t*, const LinkRec*,
                                               const double*, float*, cudaStream_t);
 template cudaError_t launch_scatter_gq<double>(const Grid&, const uint32_t*, const LinkRec*,

@@ -87,6 +87,23 @@ int adjoint_seed(const lbm_sim* s, void* nu, cudaStream_t st) {
   return cuda_check(e, "adjoint seed");
 }
 
+// nu_N = Z^T g for a cotangent g on the final f_N (compute type).
+int adjoint_seed_dense(const lbm_sim* s, const void* g, void* nu, cudaStream_t st) {
+  cudaError_t e;
+  if (is_fp64(s)) {
+    StepArgs<double> a;
+    fill_args<double>(s, a);
+    e = launch_adjoint_seed_dense<double>(a, static_cast<const double*>(g),
+                                          static_cast<double*>(nu), st);
+  } else {
+    StepArgs<float> a;
+    fill_args<float>(s, a);
+    e = launch_adjoint_seed_dense<float>(a, static_cast<const float*>(g),
+                                         static_cast<float*>(nu), st);
+  }
+  return cuda_check(e, "adjoint dense seed");
+}
+
 void free_geometry(lbm_sim* s) {
   cudaFree(s->tag);
   cudaFree(s->rec);
@@ -540,20 +557,16 @@ int lbm_run(lbm_sim* s, int n_steps, int sample_every, double* samples, void* st
   return LBM_OK;
 }
 
-int lbm_cd_and_grad(lbm_sim* s, int n_steps, int checkpoint_every, double* cd_host,
-                    double* dcd_dr_host, void* dcd_dq, void* dcd_df0, void* stream) {
-  if (!s || !cd_host || !dcd_dr_host) return set_error(LBM_ERR_ARG, "lbm_cd_and_grad: null argument");
-  if (n_steps < 1) return set_error(LBM_ERR_ARG, "lbm_cd_and_grad: n_steps < 1");
-  if (!s->have_geometry) return set_error(LBM_ERR_STATE, "lbm_cd_and_grad: set a geometry first");
-  if (s->state_is_S)
-    return set_error(LBM_ERR_STATE, "lbm_cd_and_grad: needs the initial state; call lbm_set_state");
-  if (s->p.guard != LBM_GUARD_OFF)
-    return set_error(LBM_ERR_UNSUPPORTED,
-                     "lbm_cd_and_grad: the stability guard is not differentiated (the reference "
-                     "gradient drivers run without it)");
-  LBM_TRY(check_align(dcd_dq, s->re_bytes, "dcd_dq"));
-  LBM_TRY(check_align(dcd_df0, s->re_bytes, "dcd_df0"));
-  cudaStream_t st = static_cast<cudaStream_t>(stream);
+namespace {
+
+// One gradient evaluation from the state set by lbm_set_state.  Without
+// `seed_f` the backward pass starts from the drag coefficient (Cd and dCd/dr
+// returned); with `seed_f`, a cotangent on the final f_N (compute type), it
+// starts from that and cd / dcd_dr are not computed.  dcd_dq / dcd_df0 (may
+// be null) receive the cotangents of q and f_0.
+int cd_and_grad_impl(lbm_sim* s, int n_steps, int checkpoint_every, double* cd_host,
+                     double* dcd_dr_host, void* dcd_dq, void* dcd_df0, cudaStream_t st,
+                     const void* seed_f) {
   const int N = n_steps;
   const size_t state_bytes = s->n * Q * s->st_bytes;
   for (int b = 0; b < 2; ++b)
@@ -626,15 +639,24 @@ int lbm_cd_and_grad(lbm_sim* s, int n_steps, int checkpoint_every, double* cd_ho
     LBM_TRY(launch(s, prev, dst, k == 0 ? SF_COLLIDE_ONLY : 0, st));
     prev = dst;
   }
-  LBM_TRY(launch(s, prev, s->nu[1], SF_STREAM_ONLY | SF_FORCE, st));
-  LBM_TRY(cuda_check(launch_force_finalize(s->partials, s->nblocks, dyn_area(s), s->scal, st), "force"));
-  LBM_TRY(cuda_check(launch_dj_dfx(s->scal, dyn_area(s), s->scal + 4, st), "dJ/dFx"));
+  if (!seed_f) {
+    // the force of f_N (the pass writes no populations: dst null)
+    LBM_TRY(launch(s, prev, nullptr, SF_STREAM_ONLY | SF_FORCE, st));
+    LBM_TRY(cuda_check(launch_force_finalize(s->partials, s->nblocks, dyn_area(s), s->scal, st),
+                       "force"));
+    LBM_TRY(cuda_check(launch_dj_dfx(s->scal, dyn_area(s), s->scal + 4, st), "dJ/dFx"));
+  } else {
+    LBM_TRY(cuda_check(cudaMemsetAsync(s->scal, 0, 8 * sizeof(double), st), "memset"));
+  }
 
   // ---- backward
   LBM_TRY(cuda_check(cudaMemsetAsync(s->gr_partials, 0, size_t(s->nblocks) * 16 * sizeof(double), st), "memset"));
   LBM_TRY(cuda_check(cudaMemsetAsync(s->gq, 0, size_t(s->gq_cap > 0 ? s->gq_cap : 1) * Q * sizeof(double), st), "memset"));
   int cur = 0;
-  LBM_TRY(adjoint_seed(s, s->nu[cur], st));
+  if (seed_f)
+    LBM_TRY(adjoint_seed_dense(s, seed_f, s->nu[cur], st));
+  else
+    LBM_TRY(adjoint_seed(s, s->nu[cur], st));
   for (int c = nseg - 1; c >= 0; --c) {
     const int a0 = seg_a(c), b0 = seg_a(c + 1);
     const void* slot0 = a0 == 0 ? s->fbuf : ckpt(c - 1);
@@ -649,7 +671,7 @@ int lbm_cd_and_grad(lbm_sim* s, int n_steps, int checkpoint_every, double* cd_ho
     for (int k = b0 - 1; k >= a0; --k) {
       const void* Sprev = (k == a0) ? slot0 : stash(k - a0);
       LBM_TRY(adjoint_launch(s, Sprev, stash(k - a0 + 1), s->nu[cur], s->nu[1 - cur], k == 0,
-                             k == N - 1, st));
+                             k == N - 1 && !seed_f, st));
       cur = 1 - cur;
     }
   }
@@ -668,6 +690,60 @@ int lbm_cd_and_grad(lbm_sim* s, int n_steps, int checkpoint_every, double* cd_ho
   LBM_TRY(cuda_check(cudaStreamSynchronize(st), "sync"));
   *cd_host = h[3];
   *dcd_dr_host = h[5];
+  return LBM_OK;
+}
+
+}  // namespace
+
+int lbm_cd_and_grad(lbm_sim* s, int n_steps, int checkpoint_every, double* cd_host,
+                    double* dcd_dr_host, void* dcd_dq, void* dcd_df0, void* stream) {
+  if (!s || !cd_host || !dcd_dr_host) return set_error(LBM_ERR_ARG, "lbm_cd_and_grad: null argument");
+  if (n_steps < 1) return set_error(LBM_ERR_ARG, "lbm_cd_and_grad: n_steps < 1");
+  if (!s->have_geometry) return set_error(LBM_ERR_STATE, "lbm_cd_and_grad: set a geometry first");
+  if (s->state_is_S)
+    return set_error(LBM_ERR_STATE, "lbm_cd_and_grad: needs the initial state; call lbm_set_state");
+  if (s->p.guard != LBM_GUARD_OFF)
+    return set_error(LBM_ERR_UNSUPPORTED,
+                     "lbm_cd_and_grad: the stability guard is not differentiated (the reference "
+                     "gradient drivers run without it)");
+  LBM_TRY(check_align(dcd_dq, s->re_bytes, "dcd_dq"));
+  LBM_TRY(check_align(dcd_df0, s->re_bytes, "dcd_df0"));
+  return cd_and_grad_impl(s, n_steps, checkpoint_every, cd_host, dcd_dr_host, dcd_dq, dcd_df0,
+                          static_cast<cudaStream_t>(stream), nullptr);
+}
+
+int lbm_vjp_run(lbm_sim* s, int n_steps, int checkpoint_every, const void* g_f_final,
+                void* g_f0, void* g_q, void* stream) {
+  if (!s || !g_f_final || !g_f0) return set_error(LBM_ERR_ARG, "lbm_vjp_run: null argument");
+  if (n_steps < 1) return set_error(LBM_ERR_ARG, "lbm_vjp_run: n_steps < 1");
+  if (!s->have_geometry) return set_error(LBM_ERR_STATE, "lbm_vjp_run: set a geometry first");
+  if (s->state_is_S)
+    return set_error(LBM_ERR_STATE, "lbm_vjp_run: needs the initial state; call lbm_set_state");
+  if (s->porosity_mode == LBM_POROSITY_SOFT)
+    return set_error(LBM_ERR_UNSUPPORTED,
+                     "lbm_vjp_run: porosity blends are differentiated by lbm_cd_and_grad only");
+  LBM_TRY(check_align(g_f_final, s->re_bytes, "g_f_final"));
+  LBM_TRY(check_align(g_f0, s->re_bytes, "g_f0"));
+  LBM_TRY(check_align(g_q, s->re_bytes, "g_q"));
+  cudaStream_t st = static_cast<cudaStream_t>(stream);
+  const bool guarded = s->p.guard != LBM_GUARD_OFF;
+  unsigned long long r0 = 0, r1 = 0;
+  if (guarded) {
+    LBM_TRY(cuda_check(cudaMemcpyAsync(&r0, s->guard_count, sizeof(r0), cudaMemcpyDeviceToHost,
+                                       st), "guard D2H"));
+    LBM_TRY(cuda_check(cudaStreamSynchronize(st), "sync"));
+  }
+  double cd = 0.0, gr = 0.0;
+  LBM_TRY(cd_and_grad_impl(s, n_steps, checkpoint_every, &cd, &gr, g_q, g_f0, st, g_f_final));
+  if (guarded) {
+    LBM_TRY(cuda_check(cudaMemcpyAsync(&r1, s->guard_count, sizeof(r1), cudaMemcpyDeviceToHost,
+                                       st), "guard D2H"));
+    LBM_TRY(cuda_check(cudaStreamSynchronize(st), "sync"));
+    if (r1 != r0)
+      return set_error(LBM_ERR_UNSUPPORTED,
+                       "lbm_vjp_run: the stability guard reset cells in these steps; the "
+                       "gradient through a reset is not provided");
+  }
   return LBM_OK;
 }
 

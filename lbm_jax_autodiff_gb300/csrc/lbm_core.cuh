@@ -213,8 +213,44 @@ template <class Re> struct IsSingle {
   static constexpr bool value = sizeof(typename ScalarOf<Re>::type) == 4;
 };
 
-__host__ __device__ __forceinline__ float lbm_sqrt(float x) { return sqrtf(x); }
+// Reciprocal and square root of the collision arithmetic in FP32 device
+// code.  LBM_FAST_MATH 0: the correctly rounded operations (multi-instruction
+// sequences); 1: the hardware approximations rcp.approx.ftz.f32 and
+// sqrt.approx.ftz.f32, one instruction each; 2 (the default): rcp.approx.f32
+// refined by one Newton step (two FMAs) and sqrt.approx.f32, without
+// flushing subnormals.  FP64 and host code round correctly.
+#ifndef LBM_FAST_MATH
+#define LBM_FAST_MATH 2
+#endif
+__host__ __device__ __forceinline__ float lbm_sqrt(float x) {
+#if defined(__CUDA_ARCH__) && LBM_FAST_MATH == 1
+  float r;
+  asm("sqrt.approx.ftz.f32 %0, %1;" : "=f"(r) : "f"(x));
+  return r;
+#elif defined(__CUDA_ARCH__) && LBM_FAST_MATH == 2
+  float r;
+  asm("sqrt.approx.f32 %0, %1;" : "=f"(r) : "f"(x));
+  return r;
+#else
+  return sqrtf(x);
+#endif
+}
 __host__ __device__ __forceinline__ double lbm_sqrt(double x) { return sqrt(x); }
+__host__ __device__ __forceinline__ float lbm_rcp(float x) {
+#if defined(__CUDA_ARCH__) && LBM_FAST_MATH == 1
+  float r;
+  asm("rcp.approx.ftz.f32 %0, %1;" : "=f"(r) : "f"(x));
+  return r;
+#elif defined(__CUDA_ARCH__) && LBM_FAST_MATH == 2
+  float r;
+  asm("rcp.approx.f32 %0, %1;" : "=f"(r) : "f"(x));
+  // Newton step r += r (1 - x r)
+  return fmaf(r, fmaf(-x, r, 1.0f), r);
+#else
+  return 1.0f / x;
+#endif
+}
+__host__ __device__ __forceinline__ double lbm_rcp(double x) { return 1.0 / x; }
 
 // Output sink of the collision routines: an array (out[i] = v) or a callable
 // out(i, v) that consumes each post-collision population as it is produced
@@ -231,7 +267,7 @@ __host__ __device__ __forceinline__ auto emit(F& out, int i, Re v) -> decltype(o
 // b > 0 ? a / b : 0, and "is any lane > 0" (a packed type overloads both).
 template <class Re>
 __host__ __device__ __forceinline__ Re div_if_pos(Re a, Re b) {
-  return b > Re(0) ? a / b : Re(0);
+  return b > Re(0) ? Re(a * lbm_rcp(b)) : Re(0);
 }
 template <class Re>
 __host__ __device__ __forceinline__ bool any_pos(Re v) {
@@ -323,7 +359,7 @@ __host__ __device__ __forceinline__ void equilibrium_vjp(const Re v[Q], Re rho, 
 template <class Re>
 __host__ __device__ __forceinline__ void macro_vjp_add(Re grho, Re gx, Re gy, Re gz, Re rho, Re ux,
                                               Re uy, Re uz, Re gf[Q]) {
-  const Re ir = Re(1) / rho;
+  const Re ir = lbm_rcp(rho);
   const Re hx = gx * ir, hy = gy * ir, hz = gz * ir;
   const Re c0 = grho - (hx * ux + hy * uy + hz * uz);
 #pragma unroll
@@ -589,7 +625,7 @@ template <class Re, class KT, class Out>
 __host__ __device__ __forceinline__ Re collide_cell_rj(const Re f[Q], Re rho, Re jx, Re jy, Re jz,
                                                        Re tau, bool mrt, bool smag, Re c18cs2,
                                                        const KT& K, Out out) {
-  const Re ir = Re(1) / rho;
+  const Re ir = lbm_rcp(rho);
   const Re ux = jx * ir, uy = jy * ir, uz = jz * ir;
   Re omega;
   if (mrt) {
@@ -600,9 +636,9 @@ __host__ __device__ __forceinline__ Re collide_cell_rj(const Re f[Q], Re rho, Re
       Re p[6], s[6];
       raw_second_moments<Re>(f, p);
       neq_stress<Re>(p, K.w, rho, ux, uy, uz, s);
-      omega = Re(1) / smag_tau<Re>(tau, c18cs2, smag_pi<Re>(s), inv_rho_eps<Re>(rho, ir));
+      omega = lbm_rcp(smag_tau<Re>(tau, c18cs2, smag_pi<Re>(s), inv_rho_eps<Re>(rho, ir)));
     } else {
-      omega = Re(1) / tau;
+      omega = lbm_rcp(tau);
     }
     mrt_relax_back<Re>(f, m, rho, ux, uy, uz, omega, K.rate, out);
   } else {
@@ -610,9 +646,9 @@ __host__ __device__ __forceinline__ Re collide_cell_rj(const Re f[Q], Re rho, Re
       Re p[6], s[6];
       raw_second_moments<Re>(f, p);
       neq_stress<Re>(p, K.w, rho, ux, uy, uz, s);
-      omega = Re(1) / smag_tau<Re>(tau, c18cs2, smag_pi<Re>(s), inv_rho_eps<Re>(rho, ir));
+      omega = lbm_rcp(smag_tau<Re>(tau, c18cs2, smag_pi<Re>(s), inv_rho_eps<Re>(rho, ir)));
     } else {
-      omega = Re(1) / tau;
+      omega = lbm_rcp(tau);
     }
     bgk_collide<Re>(f, rho, ux, uy, uz, omega, K.w, out);
   }
@@ -694,7 +730,7 @@ __host__ __device__ __forceinline__ void cell_scalars(const Re f[Q], CellScalars
   c.rho = density<Re>(f);
   Re jx, jy, jz;
   momentum<Re>(f, jx, jy, jz);
-  const Re ir = Re(1) / c.rho;
+  const Re ir = lbm_rcp(c.rho);
   c.ux = jx * ir;
   c.uy = jy * ir;
   c.uz = jz * ir;
@@ -710,7 +746,7 @@ __host__ __device__ __forceinline__ void collide_vjp_s(const CellScalars<Re>& cs
                                                        Re c18cs2, const KT& K,
                                                        Re* g_tau_out) {
   const Re rho = cs.rho, ux = cs.ux, uy = cs.uy, uz = cs.uz;
-  const Re ir = Re(1) / rho;
+  const Re ir = lbm_rcp(rho);
   Re sst[6];
   Re tau_eff = tau, pi = Re(0), R = Re(0), inv_rr = Re(0);
   if (smag) {
@@ -720,7 +756,7 @@ __host__ __device__ __forceinline__ void collide_vjp_s(const CellScalars<Re>& cs
     R = lbm_sqrt(tau * tau + c18cs2 * pi * inv_rr);
     tau_eff = Re(0.5) * (tau + R);
   }
-  const Re omega = Re(1) / tau_eff;
+  const Re omega = lbm_rcp(tau_eff);
   const bool want_omega = smag || g_tau_out != nullptr;
   Re g_omega = Re(0);
   Re grho = 0, gx = 0, gy = 0, gz = 0;

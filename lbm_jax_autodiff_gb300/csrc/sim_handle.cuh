@@ -68,6 +68,9 @@ template <class St>
 cudaError_t launch_adjoint(const AdjArgs<typename Storage<St>::Re>& A, bool mrt, cudaStream_t st);
 template <class Re>
 cudaError_t launch_adjoint_seed(const StepArgs<Re>& a, const double* dj, Re* nu, cudaStream_t st);
+template <class Re>
+cudaError_t launch_adjoint_seed_dense(const StepArgs<Re>& a, const Re* g, Re* nu,
+                                      cudaStream_t st);
 cudaError_t launch_dj_dfx(const double* fcd, double dyn_area, double* g, cudaStream_t st);
 cudaError_t launch_reduce_sum(const double* part, int n, double* out, cudaStream_t st);
 template <class Re>

@@ -92,9 +92,12 @@ __device__ __forceinline__ void step_body(const StepArgs<typename Storage<St>::R
     }
 
     if (fl & SF_STREAM_ONLY) {
+      // (a null dst: only the force of this pass is wanted)
       Re* fo = static_cast<Re*>(a.dst);
+      if (fo) {
 #pragma unroll
-      for (int i = 0; i < Q; ++i) fo[i * N + idx] = f[i];
+        for (int i = 0; i < Q; ++i) fo[i * N + idx] = f[i];
+      }
     } else {
       if ((fl & SF_GUARD_PRE) && unstable_rj<Re>(rho, jx, jy, jz)) {
 #pragma unroll

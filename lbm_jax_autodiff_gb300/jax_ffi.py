@@ -28,6 +28,8 @@ TARGETS = [
     "compute_density_vjp", "compute_velocity_vjp", "equilibrium_vjp", "bgk_vjp", "mrt_vjp",
     "smagorinsky_tau_vjp", "soft_bounce_back_vjp", "stream_vjp", "zou_he_inlet_vjp",
     "zou_he_outlet_vjp", "momentum_exchange_vjp",
+    # fused solver: n steps with sampled Cd; Cd and dCd/dr from the adjoint
+    "run", "cd_and_grad",
 ]
 
 XLA_SIGNATURE = [ctypes.c_void_p, ctypes.POINTER(ctypes.c_void_p), ctypes.c_char_p,
@@ -43,6 +45,31 @@ def descriptor(nx, ny, nz, dtype_code, flags=0, periodic_yz=1, tau_field=0, u_fa
             has_rho_target]
     dbl = [float(tau), float(cs), float(u[0]), float(u[1]), float(u[2]), float(rho)]
     return "lbm1 " + " ".join(str(int(v)) for v in ints) + " " + " ".join(v.hex() for v in dbl)
+
+
+class LBMXlaFusedDescC(ctypes.Structure):
+    """lbm_xla_fused_desc (include/lbm_gb300.h)."""
+    _fields_ = [
+        ("params", nat.LBMParamsC),
+        ("sphere", nat.LBMSphereC),
+        ("n_steps", ctypes.c_int32),
+        ("sample_every", ctypes.c_int32),
+        ("checkpoint_every", ctypes.c_int32),
+        ("pad", ctypes.c_int32),
+    ]
+
+
+def fused_descriptor(params, sphere, n_steps, sample_every=0, checkpoint_every=0):
+    """Raw bytes of lbm_xla_fused_desc: params from solver.params_struct,
+    sphere from solver.sphere_struct (its radius is replaced by the radius
+    operand at run time)."""
+    d = LBMXlaFusedDescC()
+    d.params = params
+    d.sphere = sphere
+    d.n_steps = int(n_steps)
+    d.sample_every = int(sample_every)
+    d.checkpoint_every = int(checkpoint_every)
+    return bytes(d)
 
 
 def xla_target(name):
@@ -279,10 +306,45 @@ def _build():
 
     momentum_exchange.defvjp(_me_fwd, _me_bwd)
 
+    def fused_run(f0, radius, desc, n_samples):
+        """(f after the steps, samples (n_samples, 4), status) of lbm_xla_run
+        (examples/10's scan of steps with a sampled Cd)."""
+        return _call("run", (_sds(f0.shape, f0.dtype), _sds((max(n_samples, 1), 4), jnp.float64),
+                             _sds((1,), jnp.int32)),
+                     f0, jnp.asarray(radius, jnp.float64).reshape(1), desc=desc)
+
+    def simulate_cd(desc):
+        """(cd_of, cd_and_grad) on the fused solver for a fixed descriptor:
+        cd_of(radius, f0) is examples/11's simulate_cd, differentiable in the
+        radius through the hand-written adjoint (jax.custom_vjp over
+        lbm_xla_cd_and_grad); cd_and_grad returns (cd, dcd_dr, dcd_dq,
+        status) as arrays."""
+
+        def cd_and_grad(radius, f0):
+            return _call("cd_and_grad", (_sds((1,), jnp.float64), _sds((1,), jnp.float64),
+                                         _sds(f0.shape, f0.dtype), _sds((1,), jnp.int32)),
+                         f0, jnp.asarray(radius, jnp.float64).reshape(1), desc=desc)
+
+        @jax.custom_vjp
+        def cd_of(radius, f0):
+            return cd_and_grad(radius, f0)[0][0]
+
+        def fwd(radius, f0):
+            cd, g, _, _ = cd_and_grad(radius, f0)
+            return cd[0], (g[0], f0)
+
+        def bwd(res, ct):
+            g, f0 = res
+            return (ct * g, jnp.zeros_like(f0))
+
+        cd_of.defvjp(fwd, bwd)
+        return cd_of, cd_and_grad
+
     return dict(compute_density=compute_density, compute_velocity=compute_velocity,
                 equilibrium=equilibrium, bgk=bgk, mrt=mrt, smagorinsky_tau=smagorinsky_tau,
                 soft_bounce_back=soft_bounce_back, stream=stream, zou_he_inlet=zou_he_inlet,
-                zou_he_outlet=zou_he_outlet, momentum_exchange=momentum_exchange)
+                zou_he_outlet=zou_he_outlet, momentum_exchange=momentum_exchange,
+                fused_run=fused_run, simulate_cd=simulate_cd)
 
 
 _fns = None
@@ -293,7 +355,7 @@ def __getattr__(name):
     global _fns
     if name in ("compute_density", "compute_velocity", "equilibrium", "bgk", "mrt",
                 "smagorinsky_tau", "soft_bounce_back", "stream", "zou_he_inlet", "zou_he_outlet",
-                "momentum_exchange"):
+                "momentum_exchange", "fused_run", "simulate_cd"):
         if _fns is None:
             _fns = _build()
         return _fns[name]

@@ -249,3 +249,57 @@ def test_cd_of_radius_autograd(cuda):
     cdo.backward()
     assert abs(cd.item() - cdo.item()) <= 1e-10 * abs(cdo.item())
     assert abs(r.grad.item() - ro.grad.item()) <= 1e-8 * abs(ro.grad.item())
+
+
+def test_simulate_gradient_vs_oracle_autograd(cuda):
+    """jax.grad through simulate (state.py:174-230) with respect to state.f and
+    state.q: the adjoint kernels (lbm_vjp_run) against FP64 autograd through
+    the oracle's step order, with the post-boundary guard (which resets no
+    cell here, so its gradient is the unguarded one)."""
+    dt = torch.float64
+    nx, ny, nz, n = 16, 8, 8, 6
+    solid, q = geometry.create_sphere(nx, ny, nz, (0.0, 0.0, 0.0), 0.7, dt)
+    g = torch.Generator().manual_seed(3)
+    f0 = drivers.initial_state(nx, ny, nz, 0.05, dt, consts_for(dt))
+    f0 = f0 + 1e-3 * torch.randn(f0.shape, generator=g, dtype=dt)
+    w = torch.randn(f0.shape, generator=g, dtype=dt)
+    cfg = drivers.StepConfig(tau=0.6, inlet=(0.05, 0.0, 0.0), collision="mrt", guard="post",
+                             smagorinsky_cs=0.1)
+    fo = f0.clone().requires_grad_(True)
+    qo = q.clone().requires_grad_(True)
+    f_or, _, resets = drivers.run(fo, qo, cfg, n, solid=solid, consts=consts_for(dt))
+    assert resets == 0
+    (f_or * w).sum().backward()
+    st = L.LBMState(f=f0.cuda().requires_grad_(True), solid=solid.cuda(),
+                    q=q.cuda().requires_grad_(True))
+    pr = L.LBMParams(tau=0.6, inlet_velocity=torch.tensor([0.05, 0.0, 0.0]), collision_mode=1,
+                     use_smagorinsky=1, smagorinsky_cs=0.1)
+    out = L.simulate(st, pr, n)
+    # FP64 fused step against the FP64 oracle: rounding only
+    assert (out.f.detach().cpu() - f_or.detach()).abs().max().item() <= 1e-9
+    (out.f * w.cuda()).sum().backward()
+    gf = st.f.grad.cpu()
+    assert (gf - fo.grad).abs().max().item() <= 1e-8 * fo.grad.abs().max().item()
+    links = q >= 0
+    gq = st.q.grad.cpu()
+    err = (gq[links] - qo.grad[links]).abs().max().item()
+    assert err <= 1e-8 * qo.grad[links].abs().max().item()
+    assert (gq[~links] == 0).all()
+
+
+def test_simulate_keeps_geometry_and_state_between_calls(cuda):
+    """A loop of simulate calls fed its own output continues from the
+    handle's state and keeps its geometry: the same f as one long run."""
+    nx, ny, nz = 24, 12, 12
+    solid, q = geometry.create_sphere(nx, ny, nz, (0.0, 0.0, 0.0), 0.6, torch.float32)
+    f0 = drivers.initial_state(nx, ny, nz, 0.05).cuda()
+    st = L.LBMState(f=f0, solid=solid.cuda(), q=q.cuda())
+    pr = L.LBMParams(tau=0.7, inlet_velocity=torch.tensor([0.05, 0.0, 0.0]), collision_mode=1)
+    one = L.simulate(st, pr, 30)
+    cur = st
+    for _ in range(3):
+        cur = L.simulate(cur, pr, 10)
+    assert torch.equal(cur.f, one.f)
+    for _ in range(5):
+        cur = L.step(cur, pr)
+    assert torch.equal(cur.f, L.simulate(st, pr, 35).f)

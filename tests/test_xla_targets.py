@@ -67,3 +67,63 @@ def test_xla_failure_fills_results_with_nan(cuda):
         ctypes.c_void_p(torch.cuda.current_stream().cuda_stream), arr, d, len(d))
     torch.cuda.synchronize()
     assert torch.isnan(force).all()
+
+
+def _fused(nx, ny, nz, tau, n, sample_every=0, K=0, **sph):
+    from lbm_jax_autodiff_gb300 import solver
+    p = solver.params_struct(nx, ny, nz, tau, collision="mrt", use_smagorinsky=True)
+    s = solver.sphere_struct(0.5, **sph)
+    return jax_ffi.fused_descriptor(p, s, n, sample_every, K)
+
+
+def _run_raw(name, bufs, d):
+    arr = (ctypes.c_void_p * len(bufs))(*[b.data_ptr() for b in bufs])
+    jax_ffi.xla_target(name)(ctypes.c_void_p(torch.cuda.current_stream().cuda_stream), arr, d,
+                             len(d))
+    torch.cuda.synchronize()
+
+
+def test_xla_fused_run_and_gradient_match_the_solver(cuda):
+    """lbm_xla_run / lbm_xla_cd_and_grad (the fused solver behind a custom
+    call) against the solver handle on the same problem, to the bit."""
+    nx, ny, nz, tau, n = 32, 16, 16, 0.56, 40
+    sph = dict(kind="sigmoid", q_mode="bouzidi", porosity="soft", sharpness=20.0)
+    sim = L.Simulation(nx, ny, nz, tau, collision="mrt", use_smagorinsky=True)
+    sim.set_sphere(0.5, **sph)
+    f0 = sim.equilibrium_state().contiguous()
+    sim.set_state(f0)
+    smp_ref = sim.run(n, sample_every=20)
+    f_ref = sim.get_state()
+    r = torch.tensor([0.5], dtype=torch.float64, device="cuda")
+    f = torch.empty_like(f0)
+    smp = torch.empty((2, 4), dtype=torch.float64, device="cuda")
+    status = torch.full((1,), -1, dtype=torch.int32, device="cuda")
+    for _ in range(2):                      # second call: handle and geometry reused
+        _run_raw("run", [f0, r, f, smp, status], _fused(nx, ny, nz, tau, n, 20, **sph))
+        assert int(status) == 0
+        assert torch.equal(f, f_ref) and torch.equal(smp, smp_ref)
+    sim.set_state(f0)
+    cd_ref, g_ref, ex = sim.cd_and_grad(n, checkpoint_every=8, dcd_dq=True)
+    cd = torch.empty(1, dtype=torch.float64, device="cuda")
+    g = torch.empty_like(cd)
+    dq = torch.empty_like(f0)
+    _run_raw("cd_and_grad", [f0, r, cd, g, dq, status], _fused(nx, ny, nz, tau, n, 0, 8, **sph))
+    assert int(status) == 0
+    assert float(cd) == cd_ref and float(g) == g_ref
+    assert torch.equal(dq, ex["dcd_dq"])
+    sim.close()
+
+
+def test_xla_fused_failure_sets_status_and_nan(cuda):
+    """An invalid configuration (tau <= 0.5): non-zero status, NaN results."""
+    from lbm_jax_autodiff_gb300 import _native as nat
+    nx, ny, nz, n = 16, 8, 8, 4
+    f0 = torch.zeros((19, nx, ny, nz), dtype=torch.float32, device="cuda")
+    r = torch.tensor([0.5], dtype=torch.float64, device="cuda")
+    cd = torch.zeros(1, dtype=torch.float64, device="cuda")
+    g = torch.zeros_like(cd)
+    dq = torch.zeros_like(f0)
+    status = torch.zeros((1,), dtype=torch.int32, device="cuda")
+    _run_raw("cd_and_grad", [f0, r, cd, g, dq, status], _fused(nx, ny, nz, 0.4, n))
+    assert int(status) == nat.LBM_ERR_ARG
+    assert torch.isnan(cd).all() and torch.isnan(g).all() and torch.isnan(dq).all()
