@@ -214,13 +214,16 @@ template <class Re> struct IsSingle {
 };
 
 // Reciprocal and square root of the collision arithmetic in FP32 device
-// code.  LBM_FAST_MATH 0: the correctly rounded operations (multi-instruction
-// sequences); 1: the hardware approximations rcp.approx.ftz.f32 and
-// sqrt.approx.ftz.f32, one instruction each; 2 (the default): rcp.approx.f32
-// refined by one Newton step (two FMAs) and sqrt.approx.f32, without
-// flushing subnormals.  FP64 and host code round correctly.
+// code.  LBM_FAST_MATH 0 (the default): the correctly rounded operations;
+// 1: the hardware approximations rcp.approx.ftz.f32 and sqrt.approx.ftz.f32;
+// 2: rcp.approx.f32 refined by one Newton step and sqrt.approx.f32.  Measured
+// at 256x128x128 (MRT + Smagorinsky sphere), 1 and 2 take the 16-bit step
+// from 92 / 94 us to 88-90 us and the FP32 step from 112.6 to 109-110 us,
+// but move the FP32 dCd/dr from 3.5e-7 to 1.6e-5 of FP64 over 2000 steps
+// (the FP16 one from 6.4e-4 to 0.9-1.9e-3), past the accuracy bars, so
+// they stay off.  FP64 and host code always round correctly.
 #ifndef LBM_FAST_MATH
-#define LBM_FAST_MATH 2
+#define LBM_FAST_MATH 0
 #endif
 __host__ __device__ __forceinline__ float lbm_sqrt(float x) {
 #if defined(__CUDA_ARCH__) && LBM_FAST_MATH == 1
