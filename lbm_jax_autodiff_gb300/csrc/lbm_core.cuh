@@ -270,7 +270,11 @@ __host__ __device__ __forceinline__ auto emit(F& out, int i, Re v) -> decltype(o
 // b > 0 ? a / b : 0, and "is any lane > 0" (a packed type overloads both).
 template <class Re>
 __host__ __device__ __forceinline__ Re div_if_pos(Re a, Re b) {
+#if LBM_FAST_MATH
   return b > Re(0) ? Re(a * lbm_rcp(b)) : Re(0);
+#else
+  return b > Re(0) ? Re(a / b) : Re(0);
+#endif
 }
 template <class Re>
 __host__ __device__ __forceinline__ bool any_pos(Re v) {

@@ -69,8 +69,7 @@ __device__ __forceinline__ V2& operator*=(V2& a, V2 b) { a = V2(a * b); return a
 __device__ __forceinline__ V2 lbm_sqrt(V2 a) { return V2(lbm_sqrt(a.v.x), lbm_sqrt(a.v.y)); }
 __device__ __forceinline__ V2 lbm_rcp(V2 a) { return V2(lbm_rcp(a.v.x), lbm_rcp(a.v.y)); }
 __device__ __forceinline__ V2 div_if_pos(V2 a, V2 b) {
-  return V2(b.v.x > 0.0f ? a.v.x * lbm_rcp(b.v.x) : 0.0f,
-            b.v.y > 0.0f ? a.v.y * lbm_rcp(b.v.y) : 0.0f);
+  return V2(div_if_pos(a.v.x, b.v.x), div_if_pos(a.v.y, b.v.y));
 }
 __device__ __forceinline__ bool any_pos(V2 v) { return v.v.x > 0.0f || v.v.y > 0.0f; }
 
