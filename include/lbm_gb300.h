@@ -47,6 +47,7 @@ typedef enum { LBM_GUARD_OFF = 0, LBM_GUARD_PRE = 1, LBM_GUARD_POST = 2 } lbm_gu
 typedef enum { LBM_POROSITY_NONE = 0, LBM_POROSITY_HARD = 1, LBM_POROSITY_SOFT = 2 } lbm_porosity;
 typedef enum { LBM_Q_HALFWAY = 0, LBM_Q_BOUZIDI = 1 } lbm_qmode;
 typedef enum { LBM_SPHERE_DIST_MASK = 0, LBM_SPHERE_SIGMOID_MASK = 1 } lbm_sphere_kind;
+typedef enum { LBM_STREAM_AB = 0, LBM_STREAM_AA = 1 } lbm_streaming;
 
 /* Solver configuration; mirrors jax_lbm LBMParams (state.py:57-84) plus the
  * storage precision and the driver-level options of the examples. */
@@ -122,6 +123,20 @@ int lbm_get_state(lbm_sim* sim, void* f, void* stream);
  * the reference's examples do every sampling interval (examples/10:93-97). */
 int lbm_set_state_host(lbm_sim* sim, const void* f_host, void* stream);
 int lbm_get_state_host(lbm_sim* sim, void* f_host, void* stream);
+
+/* Streaming scheme of lbm_run / lbm_get_state (the states they produce are
+ * the same):
+ *  - LBM_STREAM_AB (default): two population buffers, read one, write the
+ *    other;
+ *  - LBM_STREAM_AA: one buffer updated in place, its layout alternating
+ *    between steps; the boundary cells keep their post-collision vector in a
+ *    small side buffer (records + x faces).  Halves the state's memory for
+ *    forward runs (the second buffer is released, and allocated again if
+ *    lbm_cd_and_grad needs it).  Periodic y/z, FP32 or FP64 storage.
+ * The pull of streaming.py:109-142 either way.  Switching with a running
+ * state discards it (LBM_ERR_STATE from lbm_run until lbm_set_state), and so
+ * does a geometry change under an AA state. */
+int lbm_set_streaming(lbm_sim* sim, int mode);
 
 /* Advance n_steps.  If sample_every > 0, after every sample_every-th step of
  * this call the momentum-exchange force and Cd are written to

@@ -28,6 +28,7 @@ LBM_POROSITY_NONE, LBM_POROSITY_HARD, LBM_POROSITY_SOFT = 0, 1, 2
 LBM_Q_HALFWAY, LBM_Q_BOUZIDI = 0, 1
 LBM_SPHERE_DIST_MASK, LBM_SPHERE_SIGMOID_MASK = 0, 1
 LBM_LOSS_CD, LBM_LOSS_TARGET_CD = 0, 1
+LBM_STREAM_AB, LBM_STREAM_AA = 0, 1
 
 
 class NativeLibraryMissing(RuntimeError):
@@ -111,6 +112,7 @@ SIGNATURES = {
     "lbm_set_state_host": [_vp, _vp, _vp],
     "lbm_get_state_host": [_vp, _vp, _vp],
     "lbm_run": [_vp, _i, _i, _vp, _vp],
+    "lbm_set_streaming": [_vp, _i],
     "lbm_cd_and_grad": [_vp, _i, _i, ctypes.POINTER(_d), ctypes.POINTER(_d), _vp, _vp, _vp],
     "lbm_get_projected_area": [_vp, ctypes.POINTER(_d)],
     "lbm_get_link_count": [_vp, ctypes.POINTER(_i), ctypes.POINTER(_i)],

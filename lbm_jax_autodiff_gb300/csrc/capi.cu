@@ -34,6 +34,55 @@ int launch(const lbm_sim* s, const void* src, void* dst, int extra_flags, cudaSt
 
 namespace {
 
+// Side buffers of the AA scheme: one S vector per boundary record and per
+// x-face cell, two copies.
+int ensure_aa(lbm_sim* s) {
+  const size_t slots = size_t(s->nrec) + size_t(2) * s->g.ny * s->g.nz;
+  if (s->sb_slots >= slots && s->sb[0] && s->sb[1]) return LBM_OK;
+  for (int b = 0; b < 2; ++b) {
+    cudaFree(s->sb[b]);
+    s->sb[b] = nullptr;
+  }
+  s->sb_slots = 0;
+  for (int b = 0; b < 2; ++b) LBM_TRY(dev_alloc(&s->sb[b], slots * Q * s->re_bytes));
+  s->sb_slots = slots;
+  return LBM_OK;
+}
+
+// The second population buffer of the A/B scheme (released in AA mode).
+int ensure_ab(lbm_sim* s) {
+  if (!s->S[1]) LBM_TRY(dev_alloc(&s->S[1], s->n * Q * s->st_bytes));
+  return LBM_OK;
+}
+
+// One AA launch from the handle's state: SF_COLLIDE_ONLY from f_0 (fbuf),
+// a step (the layout flips), or SF_STREAM_ONLY into f_out (state unchanged).
+template <class Re>
+int aa_launch_t(lbm_sim* s, int extra, void* f_out, cudaStream_t st) {
+  StepArgs<Re> a;
+  fill_args<Re>(s, a);
+  a.flags |= extra;
+  a.src = (extra & SF_COLLIDE_ONLY) ? s->fbuf : nullptr;
+  a.dst = (extra & SF_STREAM_ONLY) ? f_out : nullptr;
+  const bool mrt = s->p.collision == LBM_MRT;
+  Re* A = static_cast<Re*>(s->S[0]);
+  const Re* sb_in = static_cast<const Re*>(s->sb[s->sb_cur]);
+  Re* sb_out = static_cast<Re*>(s->sb[1 - s->sb_cur]);
+  LBM_TRY(cuda_check(launch_step_aa<Re>(a, A, sb_in, sb_out, s->nrec, s->aa_layout_l != 0, mrt, st),
+                     "k_step_aa launch"));
+  if (!(extra & SF_STREAM_ONLY)) {
+    s->sb_cur = 1 - s->sb_cur;
+    s->aa_layout_l = (extra & SF_COLLIDE_ONLY) ? 1 : 1 - s->aa_layout_l;
+  }
+  return LBM_OK;
+}
+
+int aa_launch(lbm_sim* s, int extra, void* f_out, cudaStream_t st) {
+  LBM_TRY(ensure_aa(s));
+  return is_fp64(s) ? aa_launch_t<double>(s, extra, f_out, st)
+                    : aa_launch_t<float>(s, extra, f_out, st);
+}
+
 template <class Re>
 int adjoint_launch_t(const lbm_sim* s, const void* S_prev, const void* S_k, const Re* nu_in,
                      Re* nu_out, int first, int last, cudaStream_t st) {
@@ -236,6 +285,8 @@ int finish_geometry(lbm_sim* s, const uint8_t* solid, const Re* q, const Re* dqd
     s->nlinks = nl;
     if ((rc = build_pair_list(s, st))) break;
     s->have_geometry = 1;
+    // the side buffers of an in-place state belong to the old records
+    if (s->aa && s->state_is_S) s->aa_needs_state = 1;
   } while (0);
   cudaFree(counter);
   cudaFree(cols);
@@ -379,6 +430,8 @@ int lbm_destroy(lbm_sim* s) {
   if (!s) return LBM_OK;
   cudaFree(s->S[0]);
   cudaFree(s->S[1]);
+  cudaFree(s->sb[0]);
+  cudaFree(s->sb[1]);
   cudaFree(s->fbuf);
   cudaFree(s->partials);
   cudaFree(s->guard_count);
@@ -471,6 +524,7 @@ int lbm_set_state(lbm_sim* s, const void* f, void* stream) {
   s->state_is_S = 0;
   s->steps = 0;
   s->fbuf_step = 0;
+  s->aa_needs_state = 0;
   return LBM_OK;
 }
 
@@ -483,6 +537,7 @@ int lbm_set_state_host(lbm_sim* s, const void* f_host, void* stream) {
   s->state_is_S = 0;
   s->steps = 0;
   s->fbuf_step = 0;
+  s->aa_needs_state = 0;
   return LBM_OK;
 }
 
@@ -493,7 +548,10 @@ int lbm_get_state_host(lbm_sim* s, void* f_host, void* stream) {
     // f of the current step is not in fbuf yet: one stream-only pass (the
     // first-step input f_0 it overwrites is no longer needed)
     if (!s->have_geometry) return set_error(LBM_ERR_STATE, "lbm_get_state_host: no geometry");
-    LBM_TRY(launch(s, s->S[s->cur], s->fbuf, SF_STREAM_ONLY, st));
+    if (s->aa)
+      LBM_TRY(aa_launch(s, SF_STREAM_ONLY, s->fbuf, st));
+    else
+      LBM_TRY(launch(s, s->S[s->cur], s->fbuf, SF_STREAM_ONLY, st));
     s->fbuf_step = s->steps;
   }
   return cuda_check(cudaMemcpyAsync(f_host, s->fbuf, s->n * Q * s->re_bytes,
@@ -509,6 +567,7 @@ int lbm_get_state(lbm_sim* s, void* f, void* stream) {
     return cuda_check(cudaMemcpyAsync(f, s->fbuf, s->n * Q * s->re_bytes, cudaMemcpyDeviceToDevice, st),
                       "state copy");
   if (!s->have_geometry) return set_error(LBM_ERR_STATE, "lbm_get_state: no geometry");
+  if (s->aa) return aa_launch(s, SF_STREAM_ONLY, f, st);
   return launch(s, s->S[s->cur], f, SF_STREAM_ONLY, st);
 }
 
@@ -529,6 +588,35 @@ int lbm_run(lbm_sim* s, int n_steps, int sample_every, double* samples, void* st
     return rel / sample_every - 1;
   };
   const long long k0 = s->steps;
+  if (s->aa_needs_state)
+    return set_error(LBM_ERR_STATE,
+                     "lbm_run: the streaming scheme changed, or the geometry changed under an "
+                     "in-place (AA) state; call lbm_set_state");
+  if (s->aa) {
+    for (int L = 1; L <= n_steps; ++L) {
+      if (!s->state_is_S) {
+        LBM_TRY(aa_launch(s, SF_COLLIDE_ONLY, nullptr, st));
+        s->state_is_S = 1;
+      } else {
+        const long long si = want_sample(s->steps, k0);
+        LBM_TRY(aa_launch(s, si >= 0 ? SF_FORCE : 0, nullptr, st));
+        if (si >= 0)
+          LBM_TRY(cuda_check(launch_force_finalize(s->partials, s->nblocks, da, samples + 4 * si,
+                                                   st),
+                             "force finalize"));
+      }
+      s->steps += 1;
+    }
+    const long long si = want_sample(s->steps, k0);
+    if (si >= 0) {
+      LBM_TRY(aa_launch(s, SF_STREAM_ONLY | SF_FORCE, s->fbuf, st));
+      s->fbuf_step = s->steps;
+      LBM_TRY(cuda_check(launch_force_finalize(s->partials, s->nblocks, da, samples + 4 * si, st),
+                         "force finalize"));
+    }
+    return LBM_OK;
+  }
+  LBM_TRY(ensure_ab(s));
   for (int L = 1; L <= n_steps; ++L) {
     if (!s->state_is_S) {
       LBM_TRY(launch(s, s->fbuf, s->S[s->cur], SF_COLLIDE_ONLY, st));
@@ -568,6 +656,7 @@ int cd_and_grad_impl(lbm_sim* s, int n_steps, int checkpoint_every, double* cd_h
                      double* dcd_dr_host, void* dcd_dq, void* dcd_df0, cudaStream_t st,
                      const void* seed_f) {
   const int N = n_steps;
+  LBM_TRY(ensure_ab(s));
   const size_t state_bytes = s->n * Q * s->st_bytes;
   for (int b = 0; b < 2; ++b)
     if (!s->nu[b]) LBM_TRY(dev_alloc(&s->nu[b], s->n * Q * s->re_bytes));
@@ -841,6 +930,34 @@ int lbm_get_adjoint_plan(lbm_sim* s, int* segment_steps, int* recomputed_steps,
   *segment_steps = s->plan_K;
   *recomputed_steps = s->plan_recompute;
   *workspace_bytes = (unsigned long long)s->plan_bytes;
+  return LBM_OK;
+}
+
+int lbm_set_streaming(lbm_sim* s, int mode) {
+  if (!s) return set_error(LBM_ERR_ARG, "lbm_set_streaming: null handle");
+  if (mode != LBM_STREAM_AB && mode != LBM_STREAM_AA)
+    return set_error(LBM_ERR_ARG, "lbm_set_streaming: mode must be LBM_STREAM_AB or LBM_STREAM_AA");
+  if (mode == LBM_STREAM_AA &&
+      (!s->g.periodic_yz || (s->p.storage != LBM_F32 && s->p.storage != LBM_F64)))
+    return set_error(LBM_ERR_UNSUPPORTED,
+                     "lbm_set_streaming: in-place streaming needs periodic y/z and FP32 or FP64 "
+                     "storage");
+  if (mode == (s->aa ? LBM_STREAM_AA : LBM_STREAM_AB)) return LBM_OK;
+  s->aa = mode == LBM_STREAM_AA;
+  // a running state's layout belongs to the old scheme: lbm_set_state first
+  if (s->state_is_S) {
+    s->state_is_S = 0;
+    s->steps = 0;
+    s->fbuf_step = -1;
+    s->aa_needs_state = 1;
+  }
+  s->aa_layout_l = 0;
+  s->sb_cur = 0;
+  if (s->aa) {
+    cudaFree(s->S[1]);     // one population buffer: the second is allocated again on demand
+    s->S[1] = nullptr;
+    s->cur = 0;
+  }
   return LBM_OK;
 }
 

@@ -15,6 +15,9 @@ namespace lbm {
 template <class St>
 cudaError_t launch_step(const StepArgs<typename Storage<St>::Re>& a, bool mrt,
                         cudaStream_t stream);
+template <class Re>
+cudaError_t launch_step_aa(const StepArgs<Re>& a, Re* A, const Re* sb_in, Re* sb_out, int nrec,
+                           bool layout_l, bool mrt, cudaStream_t st);
 cudaError_t launch_force_finalize(const double* part, int nblocks, double dyn_area, double* out,
                                   cudaStream_t stream);
 
@@ -123,6 +126,14 @@ struct lbm_sim {
   int plan_recompute = 0;
   size_t plan_bytes = 0;
   size_t workspace_limit = 0;  // cap on the population workspace of the automatic plan (0: none)
+  // in-place ("AA") streaming of lbm_run: one population buffer S[0] in
+  // layout L or P, side buffers of the boundary cells' S (step_aa.cu)
+  int aa = 0;
+  int aa_layout_l = 0;       // S[0] holds layout L (else P)
+  int aa_needs_state = 0;    // the geometry changed under an AA state
+  void* sb[2] = {nullptr, nullptr};
+  int sb_cur = 0;            // side buffer holding the current step's values
+  size_t sb_slots = 0;
 };
 
 // Longest segment length K in [1, N] whose workspace, ceil(N/K) - 1 + K

@@ -212,6 +212,13 @@ class Simulation:
                                    exact=bool(self._params.exact_constants))
 
     # -- stepping -----------------------------------------------------------
+    def set_streaming(self, mode):
+        """"ab" (two population buffers, the default) or "aa" (one buffer
+        updated in place: half the state memory of a forward run; periodic
+        y/z, FP32 / FP64 storage).  Set the state again after switching."""
+        nat.call("lbm_set_streaming", self._h,
+                 {"ab": nat.LBM_STREAM_AB, "aa": nat.LBM_STREAM_AA}[mode])
+
     def run(self, n_steps, sample_every=0, samples=None):
         """Advance n_steps.  With sample_every > 0 returns a (n_samples, 4)
         float64 CUDA tensor of (Fx, Fy, Fz, Cd) after every sample_every-th step."""
