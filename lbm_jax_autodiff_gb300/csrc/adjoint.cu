@@ -347,6 +347,42 @@ template <class St> struct AdjPairArgs {
 
 constexpr int kAdjPairBlock = 128;   // 256 cells per block, as k_adjoint
 
+// Per-direction base pointers of a pair launch (as pair_pull / pair_out of
+// the forward step): from the state pointers and grid sizes, or from the
+// argument block's pointer tables with LBM_PAIR_PTR_ARITH 0.
+#ifndef LBM_PAIR_PTR_ARITH
+#define LBM_PAIR_PTR_ARITH 1
+#endif
+template <class St>
+__device__ __forceinline__ long long dir_off(const AdjPairArgs<St>& P, int i) {
+  const Grid& g = P.A.s.g;
+  return (long long)(ex(i) * g.ny * g.nz + ey(i) * g.nz + ez(i));
+}
+template <class St>
+__device__ __forceinline__ const St* adj_pull(const AdjPairArgs<St>& P, int i) {
+#if LBM_PAIR_PTR_ARITH
+  return static_cast<const St*>(P.A.s.src) + (long long)i * P.A.s.g.n - dir_off(P, i);
+#else
+  return P.pull[i];
+#endif
+}
+template <class St>
+__device__ __forceinline__ const float* adj_push(const AdjPairArgs<St>& P, int j) {
+#if LBM_PAIR_PTR_ARITH
+  return P.A.nu_in + (long long)j * P.A.s.g.n + dir_off(P, j);
+#else
+  return P.push[j];
+#endif
+}
+template <class St>
+__device__ __forceinline__ float* adj_out(const AdjPairArgs<St>& P, int i) {
+#if LBM_PAIR_PTR_ARITH
+  return P.A.nu_out + (long long)i * P.A.s.g.n;
+#else
+  return P.out[i];
+#endif
+}
+
 #ifndef LBM_ADJ_PAIR_MINB
 #define LBM_ADJ_PAIR_MINB 4
 #endif
@@ -411,7 +447,7 @@ __device__ __forceinline__ double adj_pair_finish(const AdjPairArgs<St>& P, int 
                     static_cast<V2*>(nullptr));
   // (x faces are listed pairs: no Zou-He transpose here)
 #pragma unroll
-  for (int i = 0; i < Q; ++i) *reinterpret_cast<float2*>(P.out[i] + idx) = mu[i].v;
+  for (int i = 0; i < Q; ++i) *reinterpret_cast<float2*>(adj_out(P, i) + idx) = mu[i].v;
   return gr;
 }
 
@@ -468,7 +504,7 @@ __device__ __forceinline__ double adjoint_pair_interior(const AdjPairArgs<St>& P
 #pragma unroll
     for (int j = 0; j < Q; ++j) {
       const int b = ey(j) == 1 ? iyp : (ey(j) == -1 ? iym : idx);
-      const float* p = P.push[j] + b;
+      const float* p = adj_push(P, j) + b;
       if (ez(j) == 0) mu[j] = V2(ldg_s(reinterpret_cast<const float2*>(p)));
       else if (ez(j) == 1) mu[j] = V2(ldg_s(p), ldg_s(p + 1 + zw1));
       else mu[j] = V2(ldg_s(p + zw0), ldg_s(p + 1));
@@ -489,7 +525,7 @@ __device__ __forceinline__ double adjoint_pair_interior(const AdjPairArgs<St>& P
 #pragma unroll
     for (int i = 0; i < Q; ++i) {
       const int b = ey(i) == 1 ? iym : (ey(i) == -1 ? iyp : idx);
-      const St* p = P.pull[i] + b;
+      const St* p = adj_pull(P, i) + b;
       const V2 so(P.soff2[cls][i]);
       if (ez(i) == 0) f[i] = Pr::ld2(p, so);
       else if (ez(i) == 1) f[i] = Pr::ld2s(p + zw0, p + 1, so);

@@ -157,6 +157,32 @@ template <class St> struct PairArgs {
 
 constexpr int kPairBlock = 128;   // 256 cells per block
 
+// Per-direction base pointers of a pair launch.  LBM_PAIR_PTR_ARITH 1: formed
+// from the two population pointers and the grid sizes (kernel parameters
+// only, the same for every thread); 0: read from the argument block's
+// per-direction pointer tables.
+#ifndef LBM_PAIR_PTR_ARITH
+#define LBM_PAIR_PTR_ARITH 1
+#endif
+template <class St>
+__device__ __forceinline__ const St* pair_pull(const PairArgs<St>& P, int i) {
+#if LBM_PAIR_PTR_ARITH
+  const Grid& g = P.a.g;
+  return static_cast<const St*>(P.a.src) + (long long)i * g.n -
+         (ex(i) * g.ny * g.nz + ey(i) * g.nz + ez(i));
+#else
+  return P.pull[i];
+#endif
+}
+template <class St>
+__device__ __forceinline__ St* pair_out(const PairArgs<St>& P, int i) {
+#if LBM_PAIR_PTR_ARITH
+  return static_cast<St*>(P.a.dst) + (long long)i * P.a.g.n;
+#else
+  return P.out[i];
+#endif
+}
+
 // Pre/post guard of state.py:161-169 on both lanes; returns the number of
 // lanes reset (to `reset`, with rho and j recomputed).
 __device__ __forceinline__ unsigned guard_pair(V2 f[Q], V2& rho, V2& jx, V2& jy, V2& jz,
@@ -184,7 +210,6 @@ __device__ __forceinline__ unsigned finish_pair(const PairArgs<St>& P, int idx, 
                                                 int z, uint32_t t0, uint32_t t1, V2 f[Q]) {
   using Pr = Pair<St>;
   const StepArgs<float>& a = P.a;
-  St* const* out = P.out;
   constexpr FixedConstsF K{};
   const int fl = a.flags;
   unsigned resets = 0;
@@ -202,7 +227,7 @@ __device__ __forceinline__ unsigned finish_pair(const PairArgs<St>& P, int idx, 
   if (!blend && !((fl & SF_SOLID_HARD) && (s0 || s1))) {
     // plain fluid pair: each post-collision population is stored as it is
     // produced, no output array stays live
-    auto store = [&](int i, V2 v) { Pr::st2(out[i] + idx, v, off(i)); };
+    auto store = [&](int i, V2 v) { Pr::st2(pair_out(P, i) + idx, v, off(i)); };
     collide_cell_rj<V2>(f, rho, jx, jy, jz, V2(a.tau), MRT, (fl & SF_SMAG) != 0, V2(a.c18cs2), K,
                         store);
     return resets;
@@ -212,14 +237,16 @@ __device__ __forceinline__ unsigned finish_pair(const PairArgs<St>& P, int idx, 
   if ((fl & SF_SOLID_HARD) && (s0 || s1)) {
 #pragma unroll
     for (int i = 0; i < Q; ++i)
-      Pr::st2(out[i] + idx, V2(s0 ? c[opp(i)].x() : c[i].x(), s1 ? c[opp(i)].y() : c[i].y()),
+      Pr::st2(pair_out(P, i) + idx,
+              V2(s0 ? c[opp(i)].x() : c[i].x(), s1 ? c[opp(i)].y() : c[i].y()),
               off(i));
   } else if (fl & (SF_SOLID_SPHERE | SF_SOLID_FIELD)) {
     // porosity field, or the sigmoid sphere's precomputed one
     const V2 p(__ldg(reinterpret_cast<const float2*>(a.porosity + idx)));
     const V2 omp = V2(1.0f) - p;
 #pragma unroll
-    for (int i = 0; i < Q; ++i) Pr::st2(out[i] + idx, omp * c[i] + p * c[opp(i)], off(i));
+    for (int i = 0; i < Q; ++i)
+      Pr::st2(pair_out(P, i) + idx, omp * c[i] + p * c[opp(i)], off(i));
   }
   return resets;
 }
@@ -293,7 +320,7 @@ __device__ __forceinline__ unsigned step_pair_interior(const PairArgs<St>& P, in
   for (int i = 0; i < Q; ++i) {
     const V2 so(P.soff2[cls][i]);
     const int b = ey(i) == 1 ? iym : (ey(i) == -1 ? iyp : idx);
-    const St* p = P.pull[i] + b;
+    const St* p = pair_pull(P, i) + b;
     if (ez(i) == 0) f[i] = Pr::ld2(p, so);
     else if (ez(i) == 1) f[i] = Pr::ld2s(p + zw0, p + 1, so);
     else f[i] = Pr::ld2s(p, p + 1 + zw1, so);
