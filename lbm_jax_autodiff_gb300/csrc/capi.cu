@@ -567,6 +567,11 @@ int lbm_get_state(lbm_sim* s, void* f, void* stream) {
     return cuda_check(cudaMemcpyAsync(f, s->fbuf, s->n * Q * s->re_bytes, cudaMemcpyDeviceToDevice, st),
                       "state copy");
   if (!s->have_geometry) return set_error(LBM_ERR_STATE, "lbm_get_state: no geometry");
+  if (s->fbuf_step == s->steps)
+    // the last run's final sample pass already wrote f of this step
+    return cuda_check(cudaMemcpyAsync(f, s->fbuf, s->n * Q * s->re_bytes, cudaMemcpyDeviceToDevice,
+                                      st),
+                      "state copy");
   if (s->aa) return aa_launch(s, SF_STREAM_ONLY, f, st);
   return launch(s, s->S[s->cur], f, SF_STREAM_ONLY, st);
 }
