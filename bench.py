@@ -317,8 +317,9 @@ def _precision_28k(n_steps):
     """Config-4 precision form: the 256x128x128 sphere over n_steps (28,000),
     time-averaged Cd in FP32, FP16, BF16 and FP64 storage with Smagorinsky
     Cs 0.1, each against FP64; and the examples/10 run (MRT without
-    Smagorinsky) in FP32 and FP16 against the published A100 result
-    1.1854 +/- 0.0705 (paper/make_convergence_figures.py:53-54)."""
+    Smagorinsky) in the same four storages, each against its FP64 run and
+    against the published A100 result 1.1854 +/- 0.0705
+    (paper/make_convergence_figures.py:53-54)."""
     out = {"steps": n_steps, "sample_every": 500}
     smag = {}
     for storage in ("fp64", "fp32", "fp16", "bf16"):
@@ -329,11 +330,14 @@ def _precision_28k(n_steps):
     out["smagorinsky_cs0.1"] = smag
     pub_mean, pub_std = 1.1854, 0.0705
     ex10 = {}
-    for storage in ("fp32", "fp16"):
+    for storage in ("fp64", "fp32", "fp16", "bf16"):
         r = _cd_time_average(storage, n_steps, False)
         r["published_cd_mean"], r["published_cd_std"] = pub_mean, pub_std
         r["deviation_in_published_std"] = (r["cd_mean"] - pub_mean) / pub_std
         ex10[storage] = r
+    ref = ex10["fp64"]["cd_mean"]
+    for storage in ("fp32", "fp16", "bf16"):
+        ex10[storage]["cd_mean_rel_err_vs_fp64"] = abs(ex10[storage]["cd_mean"] - ref) / abs(ref)
     out["examples10_no_smagorinsky"] = ex10
     return out
 
@@ -634,11 +638,12 @@ def run_profile_case(spec):
     """A small fixed workload for ncu captures of one kernel family (no
     timing, no JSON line):
 
-      NXxNYxNZ:STORAGE:STEPS[:grad]  the bench step (MRT + Smagorinsky Cs 0.1,
-          pre-collision guard, dist-mask Bouzidi sphere r = 0.5 world at the
-          domain centre, Re 100 on D = nx/8) for STEPS steps; with ``grad`` one
-          dCd/dr evaluation over STEPS steps instead (guard off, segment
-          STEPS/4: forward, recompute and adjoint kernels);
+      NXxNYxNZ:STORAGE:STEPS[:grad|:aa]  the bench step (MRT + Smagorinsky
+          Cs 0.1, pre-collision guard, dist-mask Bouzidi sphere r = 0.5 world
+          at the domain centre, Re 100 on D = nx/8) for STEPS steps; with
+          ``grad`` one dCd/dr evaluation over STEPS steps instead (guard off,
+          segment STEPS/4: forward, recompute and adjoint kernels); with ``aa``
+          the steps run with in-place streaming (k_step_aa);
       batch:COUNT:STEPS  one batched gradient evaluation (no graph) of the
           first COUNT instances of the batched workload, segment STEPS/2.
     """
@@ -662,11 +667,14 @@ def run_profile_case(spec):
     storage = parts[1] if len(parts) > 1 else "fp32"
     steps = int(parts[2]) if len(parts) > 2 else 8
     grad = len(parts) > 3 and parts[3] == "grad"
+    aa = len(parts) > 3 and parts[3] == "aa"
     tau = 3 * U * (nx / 8.0) / RE + 0.5
     sim = Simulation(nx, ny, nz, tau, collision="mrt", storage=storage, use_smagorinsky=True,
                      smagorinsky_cs=CS, guard="off" if grad else "pre",
                      inlet_velocity=(U, 0.0, 0.0))
     sim.set_sphere(0.5, kind="dist", q_mode="bouzidi", porosity="hard")
+    if aa:
+        sim.set_streaming("aa")
     sim.set_state(sim.equilibrium_state())
     if grad:
         cd, g = sim.cd_and_grad(steps, checkpoint_every=max(1, steps // 4))

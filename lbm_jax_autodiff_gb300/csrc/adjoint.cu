@@ -348,10 +348,10 @@ template <class St> struct AdjPairArgs {
 constexpr int kAdjPairBlock = 128;   // 256 cells per block, as k_adjoint
 
 // Per-direction base pointers of a pair launch (as pair_pull / pair_out of
-// the forward step): from the state pointers and grid sizes, or from the
-// argument block's pointer tables with LBM_PAIR_PTR_ARITH 0.
+// the forward step): from the argument block's pointer tables, or with
+// LBM_PAIR_PTR_ARITH 1 from the state pointers and grid sizes.
 #ifndef LBM_PAIR_PTR_ARITH
-#define LBM_PAIR_PTR_ARITH 1
+#define LBM_PAIR_PTR_ARITH 0
 #endif
 template <class St>
 __device__ __forceinline__ long long dir_off(const AdjPairArgs<St>& P, int i) {

@@ -62,10 +62,18 @@ __global__ void __launch_bounds__(256, sizeof(Re) == 8 ? 2 : 4)
     const int slot = sb_slot(g, aa.nrec, tag, x, y, z);
     const Re* own = slot >= 0 ? aa.sb_in + size_t(slot) * Q : nullptr;
     const int nyz = g.ny * g.nz;
-    // neighbour x + d (d in {-1, 0, 1} per axis), y and z periodic
+    // index offsets of y - 1, y + 1, z - 1, z + 1 (periodic), once per cell;
+    // nbr(d) = neighbour x + d for d in {-1, 0, 1} per axis
+    const int oym = y == 0 ? (g.ny - 1) * g.nz : -g.nz;
+    const int oyp = y == g.ny - 1 ? -(g.ny - 1) * g.nz : g.nz;
+    const int ozm = z == 0 ? g.nz - 1 : -1;
+    const int ozp = z == g.nz - 1 ? 1 - g.nz : 1;
     auto nbr = [&](int dx, int dy, int dz) {
-      return ((x + dx) * g.ny + wrapi(y + dy, g.ny)) * g.nz + wrapi(z + dz, g.nz);
+      return idx + dx * nyz + (dy < 0 ? oym : (dy > 0 ? oyp : 0)) +
+             (dz < 0 ? ozm : (dz > 0 ? ozp : 0));
     };
+    // interior x: every pull source and push target lies in the grid
+    const bool xin = x > 0 && x < g.nx - 1;
     Re f[Q];
 
     if (fl & SF_COLLIDE_ONLY) {
@@ -75,15 +83,21 @@ __global__ void __launch_bounds__(256, sizeof(Re) == 8 ? 2 : 4)
     } else {
       // pull (streaming.py:109-142): x never periodic, out-of-range x sources
       // keep the cell's own S_i(x) (side buffer of the x faces)
+      if (xin) {
 #pragma unroll
-      for (int i = 0; i < Q; ++i) {
-        const int sx = x - ex(i);
-        if (sx < 0 || sx >= g.nx) {
-          f[i] = own[i];
-        } else if (LAYOUT_L) {
-          f[i] = aa.A[opp(i) * N + nbr(-ex(i), -ey(i), -ez(i))];
-        } else {
-          f[i] = aa.A[i * N + idx];
+        for (int i = 0; i < Q; ++i)
+          f[i] = LAYOUT_L ? aa.A[opp(i) * N + nbr(-ex(i), -ey(i), -ez(i))] : aa.A[i * N + idx];
+      } else {
+#pragma unroll
+        for (int i = 0; i < Q; ++i) {
+          const int sx = x - ex(i);
+          if (sx < 0 || sx >= g.nx) {
+            f[i] = own[i];
+          } else if (LAYOUT_L) {
+            f[i] = aa.A[opp(i) * N + nbr(-ex(i), -ey(i), -ez(i))];
+          } else {
+            f[i] = aa.A[i * N + idx];
+          }
         }
       }
       // Bouzidi on the cell's wall links (streaming.py:148-183)
@@ -187,15 +201,20 @@ __global__ void __launch_bounds__(256, sizeof(Re) == 8 ? 2 : 4)
 #pragma unroll
         for (int i = 0; i < Q; ++i) s[i] = c[i];
       }
+      if (!LAYOUT_L || (fl & SF_COLLIDE_ONLY)) {
 #pragma unroll
-      for (int i = 0; i < Q; ++i) {
-        if (LAYOUT_L && !(fl & SF_COLLIDE_ONLY)) {
-          // layout P: S_i(x) at A[i][x + e_i]; values leaving through an x
-          // face are not stored (the face cells keep theirs in the side buffer)
+        for (int i = 0; i < Q; ++i) aa.A[opp(i) * N + idx] = s[i];     // layout L
+      } else if (xin) {
+        // layout P: S_i(x) at A[i][x + e_i]
+#pragma unroll
+        for (int i = 0; i < Q; ++i) aa.A[i * N + nbr(ex(i), ey(i), ez(i))] = s[i];
+      } else {
+        // values leaving through an x face are not stored (the face cells
+        // keep theirs in the side buffer)
+#pragma unroll
+        for (int i = 0; i < Q; ++i) {
           const int tx = x + ex(i);
           if (tx >= 0 && tx < g.nx) aa.A[i * N + nbr(ex(i), ey(i), ez(i))] = s[i];
-        } else {
-          aa.A[opp(i) * N + idx] = s[i];     // layout L
         }
       }
       if (slot >= 0) {

@@ -108,3 +108,10 @@ def test_workspace_limits_reject_null_handles(lib):
     assert L.lbm_set_workspace_limit(None, 1 << 30) == nat.LBM_ERR_ARG
     assert L.lbm_batch_set_workspace_limit(None, 1 << 30) == nat.LBM_ERR_ARG
     assert b"null handle" in L.lbm_last_error()
+
+
+def test_streaming_setter_rejects_null_handles(lib):
+    from lbm_jax_autodiff_gb300 import _native as nat
+    L = nat.load()
+    assert L.lbm_set_streaming(None, nat.LBM_STREAM_AA) == nat.LBM_ERR_ARG
+    assert b"null handle" in L.lbm_last_error()
