@@ -255,6 +255,54 @@ def _time_steps(sim, steps, warmup, barrier):
     return e0.elapsed_time(e1) / 1e3
 
 
+def _state_api_rate(n_steps=200):
+    """The reference-shaped functional API (state.py step / simulate) on the
+    bench workload in FP32 with the post-BC guard (state.py:161-169): us per
+    step of one simulate(state, params, n) call and of a loop of step()
+    calls, beside Simulation.run on the same handle parameters.  Each step()
+    returns the reference f, which takes a stream-only pass per call besides
+    the step itself."""
+    import torch
+    from lbm_jax_autodiff_gb300 import Simulation
+    from lbm_jax_autodiff_gb300.geometry.primitives import create_sphere
+    from lbm_jax_autodiff_gb300.state import LBMParams, LBMState, simulate, step
+    solid, q = create_sphere(NX, NY, NZ, (0.0, 0.0, 0.0), 0.5)
+    solid = solid.to(torch.int32)
+    sim = Simulation(NX, NY, NZ, TAU, collision="mrt", use_smagorinsky=True, smagorinsky_cs=CS,
+                     periodic_yz=True, guard="post", inlet_velocity=(U, 0.0, 0.0))
+    sim.set_mask(solid, q=q)
+    f0 = sim.equilibrium_state().cuda()
+    sim.set_state(f0)
+
+    def timed(fn):
+        torch.cuda.synchronize()
+        t0 = time.perf_counter()
+        fn()
+        torch.cuda.synchronize()
+        return (time.perf_counter() - t0) / n_steps * 1e6
+
+    sim.run(10)
+    t_run = timed(lambda: sim.run(n_steps))
+    sim.close()
+    params = LBMParams(tau=TAU, inlet_velocity=(U, 0.0, 0.0), collision_mode=1,
+                       use_smagorinsky=1, smagorinsky_cs=CS, periodic_yz=True)
+    state = LBMState(f=f0, solid=solid, q=q)
+    simulate(state, params, 10)                    # handle and geometry built once
+
+    def loop():
+        st = state
+        for _ in range(n_steps):
+            st = step(st, params)
+
+    t_sim = timed(lambda: simulate(state, params, n_steps))
+    t_step = timed(loop)
+    return {"steps": n_steps, "run_us_per_step": round(t_run, 2),
+            "simulate_us_per_step": round(t_sim, 2), "step_loop_us_per_step": round(t_step, 2),
+            "simulate_over_run": round(t_sim / t_run, 3), "step_loop_over_run": round(t_step / t_run, 3),
+            "note": "host wall time; each step() call returns the reference f (a stream-only "
+                    "pass besides the step), simulate() returns it once per call"}
+
+
 def _grad_rate(storage, n_steps, reps, barrier, max_over_ranks, peak, ws):
     """dCd/dr (bouzidi_hard sphere, MRT + Smagorinsky, no guard) over n_steps:
     forward with checkpoints, recompute, adjoint; workspace sized to free HBM."""
@@ -564,6 +612,9 @@ def run_ours(args):
         "note": "lbm_set_streaming(LBM_STREAM_AA): one 319 MB state buffer (two for the headline)",
     }
 
+    # the reference-shaped functional API (step / simulate) on the same workload
+    state_api = _state_api_rate()
+
     # shape gradient: dCd/dr evaluations per second over a 2000-step window
     grad = {}
     if not args.no_grad:
@@ -626,6 +677,7 @@ def run_ours(args):
             "grad": grad,
             "batch": batch,
             "precision_28k": precision,
+            "state_api": state_api,
             "cd_last_sample": cd_last,
         }
         print(json.dumps(line))

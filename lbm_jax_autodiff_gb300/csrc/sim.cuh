@@ -349,11 +349,15 @@ struct NbrOff {
 // post-collision populations S_{k-1}: pull (streaming.py:109-142), Bouzidi on
 // the cell's wall links (streaming.py:148-183), Zou-He inlet/outlet
 // (boundary.py:35-200).
+// `tab` (optional): per-direction pull bases src + i N - (e_x nyz + e_y nz +
+// e_z) from the launch's argument block, so an interior pull address is one
+// table entry plus the cell index and its y / z wrap corrections.
 template <class St>
 __device__ __forceinline__ void pull_post_bc(const StepArgs<typename Storage<St>::Re>& a,
                                              const St* __restrict__ src, int idx, int x, int y,
                                              int z, uint32_t tag,
-                                             typename Storage<St>::Re f[Q]) {
+                                             typename Storage<St>::Re f[Q],
+                                             const St* const* tab = nullptr) {
   using Re = typename Storage<St>::Re;
   using S = Storage<St>;
   const Grid& g = a.g;
@@ -363,7 +367,19 @@ __device__ __forceinline__ void pull_post_bc(const StepArgs<typename Storage<St>
   constexpr bool offs = sizeof(St) == 2;
   const NearMask M(g, a.near, x, y, z, 1);
   const int cls = offs ? M.cls(1) : 0;
-  if (!O.face && cls != 2) {
+  if (!O.face && cls != 2 && tab) {
+    const int nyz = g.ny * g.nz;
+    const int wym = y == 0 ? nyz : 0;             // e_y = +1 pulls y - 1
+    const int wyp = y == g.ny - 1 ? -nyz : 0;     // e_y = -1 pulls y + 1
+    const int wzm = z == 0 ? g.nz : 0;            // e_z = +1 pulls z - 1
+    const int wzp = z == g.nz - 1 ? -g.nz : 0;    // e_z = -1 pulls z + 1
+#pragma unroll
+    for (int i = 0; i < Q; ++i) {
+      const int b = idx + (ey(i) == 1 ? wym : (ey(i) == -1 ? wyp : 0)) +
+                    (ez(i) == 1 ? wzm : (ez(i) == -1 ? wzp : 0));
+      f[i] = S::ld(tab[i] + b, cls ? a.soff_near[i] : a.soff[i]);
+    }
+  } else if (!O.face && cls != 2) {
 #pragma unroll
     for (int i = 0; i < Q; ++i)
       f[i] = S::ld(src + i * N + O.pull(i, idx), cls ? a.soff_near[i] : a.soff[i]);

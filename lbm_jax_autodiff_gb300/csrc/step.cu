@@ -36,8 +36,17 @@ namespace lbm {
 
 // One block of the fused step: cells [block * blockDim.x, +blockDim.x) of the
 // grid `a` describes; the force partial of the block goes to slot `block`.
+// Per-direction pointers of a k_step launch: pull[i] + idx is the interior
+// pull source x - e_i of cell idx (before y / z wrap), out[i] + idx its slot
+// in S_k.
+template <class St> struct CellTabs {
+  const St* pull[Q];
+  St* out[Q];
+};
+
 template <class St, bool MRT>
-__device__ __forceinline__ void step_body(const StepArgs<typename Storage<St>::Re>& a, int block) {
+__device__ __forceinline__ void step_body(const StepArgs<typename Storage<St>::Re>& a, int block,
+                                          const CellTabs<St>* T = nullptr) {
   using Re = typename Storage<St>::Re;
   using S = Storage<St>;
   const Grid& g = a.g;
@@ -59,7 +68,8 @@ __device__ __forceinline__ void step_body(const StepArgs<typename Storage<St>::R
 #pragma unroll
       for (int i = 0; i < Q; ++i) f[i] = __ldg(f0 + i * N + idx);
     } else {
-      pull_post_bc<St>(a, static_cast<const St*>(a.src), idx, x, y, z, tag, f);
+      pull_post_bc<St>(a, static_cast<const St*>(a.src), idx, x, y, z, tag, f,
+                       T ? T->pull : nullptr);
     }
 
     Re rho = density<Re>(f);
@@ -114,20 +124,20 @@ __device__ __forceinline__ void step_body(const StepArgs<typename Storage<St>::R
         collide_cell_rj<Re>(f, rho, jx, jy, jz, a.tau, MRT, (fl & SF_SMAG) != 0, a.c18cs2, a.K, c);
 
       St* dst = static_cast<St*>(a.dst);
+      auto out = [&](int i) { return T ? T->out[i] + idx : dst + i * N + idx; };
       const bool nr = in_near(a.near, x, y, z);
       if ((fl & SF_SOLID_HARD) && (tag & TAG_SOLID)) {
 #pragma unroll
-        for (int i = 0; i < Q; ++i)
-          S::st(dst + i * N + idx, c[opp(i)], nr ? a.soff_near[i] : a.soff[i]);
+        for (int i = 0; i < Q; ++i) S::st(out(i), c[opp(i)], nr ? a.soff_near[i] : a.soff[i]);
       } else if (fl & (SF_SOLID_SPHERE | SF_SOLID_FIELD)) {
         const Re p = a.porosity[idx];   // field, or the sigmoid sphere's precomputed one
         const Re omp = Re(1) - p;
 #pragma unroll
         for (int i = 0; i < Q; ++i)
-          S::st(dst + i * N + idx, omp * c[i] + p * c[opp(i)], nr ? a.soff_near[i] : a.soff[i]);
+          S::st(out(i), omp * c[i] + p * c[opp(i)], nr ? a.soff_near[i] : a.soff[i]);
       } else {
 #pragma unroll
-        for (int i = 0; i < Q; ++i) S::st(dst + i * N + idx, c[i], nr ? a.soff_near[i] : a.soff[i]);
+        for (int i = 0; i < Q; ++i) S::st(out(i), c[i], nr ? a.soff_near[i] : a.soff[i]);
       }
     }
   }
@@ -139,9 +149,20 @@ __device__ __forceinline__ void step_body(const StepArgs<typename Storage<St>::R
   }
 }
 
+// LBM_STEP_TABLES 1: k_step takes per-direction pointer tables (CellTabs)
+// for its interior pulls and its stores.
+#ifndef LBM_STEP_TABLES
+#define LBM_STEP_TABLES 1
+#endif
+
+#ifndef LBM_STEP_MINB
+#define LBM_STEP_MINB 4
+#endif
+
 template <class St, bool MRT>
-__global__ void __launch_bounds__(256, sizeof(St) == 8 ? 2 : 4) k_step(const StepArgs<typename Storage<St>::Re> a) {
-  step_body<St, MRT>(a, blockIdx.x);
+__global__ void __launch_bounds__(256, sizeof(St) == 8 ? 2 : LBM_STEP_MINB)
+    k_step(const StepArgs<typename Storage<St>::Re> a, const CellTabs<St> T) {
+  step_body<St, MRT>(a, blockIdx.x, LBM_STEP_TABLES ? &T : nullptr);
 }
 
 // Per-direction pointers of one pair launch: pull[i] + idx is the interior
@@ -462,10 +483,23 @@ cudaError_t launch_step(const StepArgs<typename Storage<St>::Re>& a, bool mrt,
   }
   const int bs = 256;
   const int nb = (a.g.n + bs - 1) / bs;
+  CellTabs<St> T;
+  {
+    const Grid& g = a.g;
+    const long long N = g.n, nyz = (long long)g.ny * g.nz;
+    for (int i = 0; i < Q; ++i) {
+      // pull bases are formed only when there is a source state (a
+      // collide-only launch reads f_0 through a.src itself)
+      T.pull[i] = a.src && !(a.flags & SF_COLLIDE_ONLY)
+                      ? static_cast<const St*>(a.src) + i * N - (ex(i) * nyz + ey(i) * g.nz + ez(i))
+                      : nullptr;
+      T.out[i] = a.dst ? static_cast<St*>(a.dst) + i * N : nullptr;
+    }
+  }
   if (mrt)
-    k_step<St, true><<<nb, bs, 0, stream>>>(a);
+    k_step<St, true><<<nb, bs, 0, stream>>>(a, T);
   else
-    k_step<St, false><<<nb, bs, 0, stream>>>(a);
+    k_step<St, false><<<nb, bs, 0, stream>>>(a, T);
   return cudaGetLastError();
 }
 
