@@ -260,8 +260,8 @@ def _state_api_rate(n_steps=200):
     bench workload in FP32 with the post-BC guard (state.py:161-169): us per
     step of one simulate(state, params, n) call and of a loop of step()
     calls, beside Simulation.run on the same handle parameters.  Each step()
-    returns the reference f, which takes a stream-only pass per call besides
-    the step itself."""
+    returns the reference f: the launch that writes it also performs the next
+    step (lbm_get_state_and_step), reading the state once."""
     import torch
     from lbm_jax_autodiff_gb300 import Simulation
     from lbm_jax_autodiff_gb300.geometry.primitives import create_sphere
@@ -299,8 +299,9 @@ def _state_api_rate(n_steps=200):
     return {"steps": n_steps, "run_us_per_step": round(t_run, 2),
             "simulate_us_per_step": round(t_sim, 2), "step_loop_us_per_step": round(t_step, 2),
             "simulate_over_run": round(t_sim / t_run, 3), "step_loop_over_run": round(t_step / t_run, 3),
-            "note": "host wall time; each step() call returns the reference f (a stream-only "
-                    "pass besides the step), simulate() returns it once per call"}
+            "note": "host wall time; each step() call returns the reference f, written by the "
+                    "launch that also performs the next step (152 + 76 B per cell), "
+                    "simulate() returns it once per call"}
 
 
 def _grad_rate(storage, n_steps, reps, barrier, max_over_ranks, peak, ws):

@@ -124,6 +124,15 @@ int lbm_get_state(lbm_sim* sim, void* f, void* stream);
 int lbm_set_state_host(lbm_sim* sim, const void* f_host, void* stream);
 int lbm_get_state_host(lbm_sim* sim, void* f_host, void* stream);
 
+/* lbm_get_state into the device buffer f, then one step (lbm_run with
+ * n_steps 1, no samples), in one launch that reads the state once: the step's
+ * pull writes the reference f it forms (after the post-BC guard) besides the
+ * next state.  For a driver that holds f between single steps, as state.py's
+ * step() does (state.py:87-171): f of step k out, the handle at step k + 1.
+ * Falls back to the two calls when there is nothing to fuse (a state just
+ * set, f already written by a sample pass, in-place streaming). */
+int lbm_get_state_and_step(lbm_sim* sim, void* f, void* stream);
+
 /* Streaming scheme of lbm_run / lbm_get_state (the states they produce are
  * the same):
  *  - LBM_STREAM_AB (default): two population buffers, read one, write the

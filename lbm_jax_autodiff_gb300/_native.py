@@ -109,6 +109,7 @@ SIGNATURES = {
     "lbm_set_inlet_profile": [_vp, _vp, _vp],
     "lbm_set_state": [_vp, _vp, _vp],
     "lbm_get_state": [_vp, _vp, _vp],
+    "lbm_get_state_and_step": [_vp, _vp, _vp],
     "lbm_set_state_host": [_vp, _vp, _vp],
     "lbm_get_state_host": [_vp, _vp, _vp],
     "lbm_run": [_vp, _i, _i, _vp, _vp],

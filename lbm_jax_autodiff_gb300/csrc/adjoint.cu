@@ -795,28 +795,31 @@ __global__ void __launch_bounds__(kAdjPairBlock, LBM_ADJ_PAIR_BATCH_MINB)
   copy_to_shared(&P.A, args + m.x);
   __syncthreads();
   const BatchInst& b = inst[m.x];
+  const float* src = static_cast<const float*>(batch_slot(b, sprev_slot));
+  const float* nu_in = static_cast<const float*>(batch_slot(b, nu_in_slot));
+  float* nu_out = static_cast<float*>(batch_slot(b, nu_out_slot));
   if (threadIdx.x == 0) {
     AdjArgs<float>& A = P.A;
-    A.s.src = batch_slot(b, sprev_slot);
+    A.s.src = src;
     A.S_k = batch_slot(b, sk_slot);
-    A.nu_in = static_cast<const float*>(batch_slot(b, nu_in_slot));
-    A.nu_out = static_cast<float*>(batch_slot(b, nu_out_slot));
+    A.nu_in = nu_in;
+    A.nu_out = nu_out;
     A.first = first;
     A.last = last;
     A.dj_dfx = b.out + 4;
     A.gr_partials = b.gr_part;
     A.gq = b.gq;
-    const Grid& g = A.s.g;
+  } else if (threadIdx.x <= Q) {
+    // the per-direction tables, one direction per thread
+    const int i = threadIdx.x - 1;
+    const Grid& g = P.A.s.g;
     const long long N = g.n, nyz = (long long)g.ny * g.nz;
-#pragma unroll
-    for (int i = 0; i < Q; ++i) {
-      const long long off = ex(i) * nyz + ey(i) * g.nz + ez(i);
-      P.pull[i] = static_cast<const float*>(A.s.src) + i * N - off;
-      P.push[i] = A.nu_in + i * N + off;
-      P.out[i] = A.nu_out + i * N;
-      P.soff2[0][i] = make_float2(0.0f, 0.0f);
-      P.soff2[1][i] = make_float2(0.0f, 0.0f);
-    }
+    const long long off = ex(i) * nyz + ey(i) * g.nz + ez(i);
+    P.pull[i] = src + i * N - off;
+    P.push[i] = nu_in + i * N + off;
+    P.out[i] = nu_out + i * N;
+    P.soff2[0][i] = make_float2(0.0f, 0.0f);
+    P.soff2[1][i] = make_float2(0.0f, 0.0f);
   }
   __syncthreads();
   const int nlist = (2 * P.A.s.spec_count + kAdjPairBlock - 1) / kAdjPairBlock;

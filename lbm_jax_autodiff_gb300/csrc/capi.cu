@@ -7,7 +7,8 @@
 
 #include "sim_handle.cuh"
 
-int launch(const lbm_sim* s, const void* src, void* dst, int extra_flags, cudaStream_t st) {
+int launch(const lbm_sim* s, const void* src, void* dst, int extra_flags, cudaStream_t st,
+           void* f_emit) {
   cudaError_t e;
   const bool mrt = s->p.collision == LBM_MRT;
   if (is_fp64(s)) {
@@ -16,6 +17,7 @@ int launch(const lbm_sim* s, const void* src, void* dst, int extra_flags, cudaSt
     a.src = src;
     a.dst = dst;
     a.flags |= extra_flags;
+    a.f_emit = f_emit;
     e = launch_step<double>(a, mrt, st);
   } else {
     StepArgs<float> a;
@@ -23,6 +25,7 @@ int launch(const lbm_sim* s, const void* src, void* dst, int extra_flags, cudaSt
     a.src = src;
     a.dst = dst;
     a.flags |= extra_flags;
+    a.f_emit = f_emit;
     switch (s->p.storage) {
       case LBM_F32: e = launch_step<float>(a, mrt, st); break;
       case LBM_F16: e = launch_step<__half>(a, mrt, st); break;
@@ -574,6 +577,28 @@ int lbm_get_state(lbm_sim* s, void* f, void* stream) {
                       "state copy");
   if (s->aa) return aa_launch(s, SF_STREAM_ONLY, f, st);
   return launch(s, s->S[s->cur], f, SF_STREAM_ONLY, st);
+}
+
+int lbm_get_state_and_step(lbm_sim* s, void* f, void* stream) {
+  if (!s || !f) return set_error(LBM_ERR_ARG, "lbm_get_state_and_step: null argument");
+  LBM_TRY(check_align(f, s->re_bytes, "f"));
+  if (!s->have_geometry)
+    return set_error(LBM_ERR_STATE, "lbm_get_state_and_step: set a geometry first");
+  if (s->aa_needs_state)
+    return set_error(LBM_ERR_STATE,
+                     "lbm_get_state_and_step: the streaming scheme changed, or the geometry "
+                     "changed under an in-place (AA) state; call lbm_set_state");
+  cudaStream_t st = static_cast<cudaStream_t>(stream);
+  if (!s->state_is_S || s->aa || s->fbuf_step == s->steps) {
+    // nothing to fuse: f is already at hand, or the in-place scheme
+    LBM_TRY(lbm_get_state(s, f, stream));
+    return lbm_run(s, 1, 0, nullptr, stream);
+  }
+  LBM_TRY(ensure_ab(s));
+  LBM_TRY(launch(s, s->S[s->cur], s->S[1 - s->cur], SF_EMIT_F, st, f));
+  s->cur = 1 - s->cur;
+  s->steps += 1;
+  return LBM_OK;
 }
 
 int lbm_run(lbm_sim* s, int n_steps, int sample_every, double* samples, void* stream) {

@@ -90,6 +90,7 @@ enum : int {
   SF_INLET_FACE = 1 << 9,     // per-(y,z) inlet velocity
   SF_NO_INLET = 1 << 10,
   SF_NO_OUTLET = 1 << 11,
+  SF_EMIT_F = 1 << 12,        // also write the post-BC f (after the post guard) to f_emit
 };
 
 template <class Re> struct SphereP {
@@ -126,6 +127,7 @@ template <class Re> struct StepArgs {
   int spec_count;
   double* force_partials; // [gridDim.x][3]
   unsigned long long* guard_count;
+  void* f_emit;           // SF_EMIT_F: the post-BC f of the pull (Re), [19][n]
 };
 
 __device__ __forceinline__ int wrapi(int v, int n) { return v < 0 ? v + n : (v >= n ? v - n : v); }

@@ -246,4 +246,5 @@ inline double dyn_area(const lbm_sim* s) {
 }
 
 // Launch one fused step of handle `s` from src to dst (defined in capi.cu).
-int launch(const lbm_sim* s, const void* src, void* dst, int extra_flags, cudaStream_t st);
+int launch(const lbm_sim* s, const void* src, void* dst, int extra_flags, cudaStream_t st,
+           void* f_emit = nullptr);

@@ -101,6 +101,13 @@ __device__ __forceinline__ void step_body(const StepArgs<typename Storage<St>::R
       }
     }
 
+    if ((fl & SF_EMIT_F) && !(fl & SF_COLLIDE_ONLY)) {
+      // the reference f of this step, as a stream-only pass would write it
+      Re* fe = static_cast<Re*>(a.f_emit);
+#pragma unroll
+      for (int i = 0; i < Q; ++i) fe[i * N + idx] = f[i];
+    }
+
     if (fl & SF_STREAM_ONLY) {
       // (a null dst: only the force of this pass is wanted)
       Re* fo = static_cast<Re*>(a.dst);
@@ -461,7 +468,7 @@ cudaError_t launch_step(const StepArgs<typename Storage<St>::Re>& a, bool mrt,
                         cudaStream_t stream) {
   if constexpr (sizeof(St) == 2) {
     if ((a.g.nz % 2) == 0 && a.spec_pairs &&
-        !(a.flags & (SF_COLLIDE_ONLY | SF_STREAM_ONLY | SF_FORCE))) {
+        !(a.flags & (SF_COLLIDE_ONLY | SF_STREAM_ONLY | SF_FORCE | SF_EMIT_F))) {
       PairArgs<St> P;
       P.a = a;
       const Grid& g = a.g;

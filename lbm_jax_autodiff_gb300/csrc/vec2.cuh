@@ -80,12 +80,6 @@ template <> struct ScalarOf<V2> { using type = float; };
 // (FP16/BF16) access; ld2s gathers two separate elements.  16-bit storage
 // holds f minus a per-direction offset w (one value per lane), as Storage<>
 // does.
-// LBM_ST2_SCALAR 1: a 16-bit store subtracts its offsets lane by lane
-// (scalar FADDs) instead of one packed subtract.
-#ifndef LBM_ST2_SCALAR
-#define LBM_ST2_SCALAR 0
-#endif
-
 template <class St> struct Pair;
 template <> struct Pair<float> {
   static __device__ __forceinline__ V2 ld2(const float* p, V2) {
@@ -122,11 +116,7 @@ template <> struct Pair<__half> {
     return V2(add_f16(ldg_s(p0), w.x()), add_f16(ldg_s(p1), w.y()));
   }
   static __device__ __forceinline__ void st2(__half* p, V2 v, V2 w) {
-#if LBM_ST2_SCALAR
-    *reinterpret_cast<__half2*>(p) = __floats2half2_rn(v.x() - w.x(), v.y() - w.y());
-#else
     *reinterpret_cast<__half2*>(p) = __float22half2_rn((v - w).v);
-#endif
   }
 };
 template <> struct Pair<__nv_bfloat16> {
@@ -139,11 +129,7 @@ template <> struct Pair<__nv_bfloat16> {
     return V2(add_bf16(ldg_s(p0), w.x()), add_bf16(ldg_s(p1), w.y()));
   }
   static __device__ __forceinline__ void st2(__nv_bfloat16* p, V2 v, V2 w) {
-#if LBM_ST2_SCALAR
-    *reinterpret_cast<__nv_bfloat162*>(p) = __floats2bfloat162_rn(v.x() - w.x(), v.y() - w.y());
-#else
     *reinterpret_cast<__nv_bfloat162*>(p) = __float22bfloat162_rn((v - w).v);
-#endif
   }
 };
 

@@ -204,6 +204,16 @@ class Simulation:
         nat.call("lbm_get_state", self._h, _ptr(out), _stream())
         return out
 
+    def get_state_and_step(self, out=None):
+        """get_state(), then run(1), in one launch that reads the state once
+        (lbm_get_state_and_step): returns f of the current step and leaves the
+        handle one step further on."""
+        if out is None:
+            out = torch.empty((19,) + self.shape, dtype=self.dtype, device="cuda")
+        _require_cuda(out, "out", self.dtype, 19 * self.n)
+        nat.call("lbm_get_state_and_step", self._h, _ptr(out), _stream())
+        return out
+
     def equilibrium_state(self, ux=None):
         """f_eq(rho=1, u=(ux,0,0)) built on the host in the reference formula."""
         from .core.lattice import equilibrium_uniform

@@ -17,7 +17,10 @@ Each solver handle keeps its geometry between calls: ``set_mask`` runs again
 only when ``state.solid`` or ``state.q`` is another tensor or was modified
 in place (its version counter moved).  A call whose ``state.f`` is the
 unmodified tensor the previous call returned continues from the handle's own
-state instead of copying f in again.
+state instead of copying f in again.  A call writes the f it returns and
+advances the handle one step further in the same launch
+(``get_state_and_step``), so a loop of ``step`` calls reads the state once
+per step.
 """
 
 import ctypes
@@ -71,6 +74,7 @@ def _handle(state, params):
         sim._geom_key = None
         sim._geom_ref = None
         sim._f_out = None
+        sim._ahead = False                 # the handle is one step past the f returned
         _CACHE[key] = sim
     return sim
 
@@ -91,14 +95,22 @@ def _set_geometry(sim, solid, q):
 
 def _run(sim, f0, n_steps, continue_from=False):
     """n_steps from f0, or from the handle's own state when f0 is the
-    unmodified tensor the handle returned last; returns a new f tensor."""
+    unmodified tensor the handle returned last; returns a new f tensor.  The
+    handle ends one step past the returned f (its pull of the next step
+    wrote it), so a continuing call has one step fewer to run."""
     last = sim._f_out
     same = (continue_from and last is not None and last[0]() is f0 and
             last[1] == f0._version)
     if not same:
         sim.set_state(f0.detach().contiguous())
-    sim.run(int(n_steps))
-    f = sim.get_state()
+        sim._ahead = False
+    m = int(n_steps) - (1 if sim._ahead else 0)
+    if m < 0:                              # n_steps == 0 on a handle already past f0
+        return f0
+    if m:
+        sim.run(m)
+    f = sim.get_state_and_step()
+    sim._ahead = True
     sim._f_out = (weakref.ref(f), f._version)
     return f
 

@@ -303,3 +303,59 @@ def test_simulate_keeps_geometry_and_state_between_calls(cuda):
     for _ in range(5):
         cur = L.step(cur, pr)
     assert torch.equal(cur.f, L.simulate(st, pr, 35).f)
+
+
+def test_get_state_and_step_equals_the_two_calls(cuda):
+    """lbm_get_state_and_step: f of the current step and one more step, to the
+    bit what get_state followed by run(1) gives, in FP32 and FP64, right after
+    set_state (the unfused fallback) and in a running state (the fused launch),
+    with the post-BC guard resetting planted cells in between."""
+    nx, ny, nz = 24, 12, 12
+    for dtype, storage in ((torch.float32, "fp32"), (torch.float64, "fp64")):
+        solid, q = geometry.create_sphere(nx, ny, nz, (0.0, 0.0, 0.0), 0.6, dtype)
+        f0 = drivers.initial_state(nx, ny, nz, 0.05, dtype, consts_for(dtype))
+        f0[:, 3, 5, 5] = float("nan")            # reset by the post-BC guard
+        sims = []
+        for _ in range(2):
+            s = L.Simulation(nx, ny, nz, 0.7, collision="mrt", storage=storage, guard="post",
+                             inlet_velocity=(0.05, 0.0, 0.0))
+            s.set_mask(solid.cuda(), q=q.cuda())
+            s.set_state(f0.cuda())
+            sims.append(s)
+        fused, plain = sims
+        bits = torch.int32 if dtype == torch.float32 else torch.int64
+
+        def same(x, y):                          # to the bit, NaN included
+            return torch.equal(x.view(bits), y.view(bits))
+
+        for k in range(4):
+            a = fused.get_state_and_step()
+            b = plain.get_state()
+            plain.run(1)
+            assert same(a, b), (storage, k)
+            fused.run(2)
+            plain.run(2)
+        assert same(fused.get_state(), plain.get_state())
+        assert fused.guard_resets == plain.guard_resets > 0
+        for s in sims:
+            s.close()
+
+
+def test_state_calls_mixed_with_restarts(cuda):
+    """simulate / step calls that continue, restart from a modified f, and run
+    zero steps give the f a fresh handle gives."""
+    nx, ny, nz = 24, 12, 12
+    solid, q = geometry.create_sphere(nx, ny, nz, (0.0, 0.0, 0.0), 0.6, torch.float32)
+    f0 = drivers.initial_state(nx, ny, nz, 0.05).cuda()
+    st = L.LBMState(f=f0, solid=solid.cuda(), q=q.cuda())
+    pr = L.LBMParams(tau=0.7, inlet_velocity=torch.tensor([0.05, 0.0, 0.0]), collision_mode=1)
+    a = L.step(L.simulate(st, pr, 3), pr)            # 4 steps, continuing
+    z = L.simulate(a, pr, 0)
+    assert torch.equal(z.f, a.f)
+    b = L.step(z, pr)                                # 5 steps
+    g = b.f.clone()
+    b.f.mul_(1.0)                                    # same values, a new version: restart
+    c = L.simulate(b, pr, 2)                         # 7 steps
+    ref = L.simulate(L.LBMState(f=g, solid=st.solid, q=st.q), pr, 2)
+    assert torch.equal(c.f, ref.f)
+    assert torch.equal(c.f, L.simulate(st, pr, 7).f)
