@@ -87,6 +87,11 @@ typedef struct lbm_sim lbm_sim;
 int lbm_api_version(void);
 const char* lbm_status_string(int status);
 const char* lbm_last_error(void);
+/* sizeof the ABI's structs, for bindings that restate them (ctypes, cgo, a
+ * JNI shim) to check their layout against: which = 0 lbm_params, 1
+ * lbm_sphere, 2 lbm_xla_desc, 3 lbm_xla_fused_desc, 4 lbm_adam; 0 for any
+ * other code. */
+size_t lbm_struct_size(int which);
 
 /* ---- fused solver handle (replaces state.py:87-230 and the examples' -----
  * ---- step_fn / lax.scan loops, e.g. examples/10:162-193) ------------------ */

@@ -102,6 +102,7 @@ SIGNATURES = {
     "lbm_api_version": [],
     "lbm_status_string": [_i],
     "lbm_last_error": [],
+    "lbm_struct_size": [_i],
     "lbm_create": [ctypes.POINTER(LBMParamsC), ctypes.POINTER(_vp)],
     "lbm_destroy": [_vp],
     "lbm_set_geometry_sphere": [_vp, ctypes.POINTER(LBMSphereC), _vp],
@@ -175,7 +176,8 @@ SIGNATURES = {
     "lbm_batch_graph_launches": [_vp, ctypes.POINTER(ctypes.c_longlong)],
     "lbm_batch_set_workspace_limit": [_vp, ctypes.c_ulonglong],
 }
-_RESTYPES = {"lbm_status_string": ctypes.c_char_p, "lbm_last_error": ctypes.c_char_p}
+_RESTYPES = {"lbm_status_string": ctypes.c_char_p, "lbm_last_error": ctypes.c_char_p,
+             "lbm_struct_size": ctypes.c_size_t}
 
 _lock = threading.Lock()
 _lib = None

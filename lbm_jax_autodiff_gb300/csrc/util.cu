@@ -48,6 +48,17 @@ extern "C" {
 
 const char* lbm_last_error(void) { return lbm::g_last_error; }
 
+size_t lbm_struct_size(int which) {
+  switch (which) {
+    case 0: return sizeof(lbm_params);
+    case 1: return sizeof(lbm_sphere);
+    case 2: return sizeof(lbm_xla_desc);
+    case 3: return sizeof(lbm_xla_fused_desc);
+    case 4: return sizeof(lbm_adam);
+    default: return 0;
+  }
+}
+
 const char* lbm_status_string(int s) {
   switch (s) {
     case LBM_OK: return "LBM_OK";

@@ -115,3 +115,20 @@ def test_streaming_setter_rejects_null_handles(lib):
     L = nat.load()
     assert L.lbm_set_streaming(None, nat.LBM_STREAM_AA) == nat.LBM_ERR_ARG
     assert b"null handle" in L.lbm_last_error()
+
+
+def test_ctypes_structs_match_the_library_layout(lib):
+    """The Python binding's restated structs have the sizes the library was
+    compiled with (lbm_struct_size), so a field added on one side only is
+    caught without a GPU."""
+    import ctypes
+
+    from lbm_jax_autodiff_gb300 import _native as nat
+    from lbm_jax_autodiff_gb300 import jax_ffi
+    L = nat.load()
+    assert L.lbm_struct_size(0) == ctypes.sizeof(nat.LBMParamsC)
+    assert L.lbm_struct_size(1) == ctypes.sizeof(nat.LBMSphereC)
+    assert L.lbm_struct_size(2) > 0
+    assert L.lbm_struct_size(3) == ctypes.sizeof(jax_ffi.LBMXlaFusedDescC)
+    assert L.lbm_struct_size(4) == ctypes.sizeof(nat.LBMAdamC)
+    assert L.lbm_struct_size(99) == 0
