@@ -363,7 +363,7 @@ def _cd_time_average(storage, n_steps, smagorinsky, sample_every=500, tail_fract
 
 
 def _precision_28k(n_steps):
-    """Config-4 precision form: the 256x128x128 sphere over n_steps (28,000),
+    """The precision form: the 256x128x128 sphere over n_steps (28,000),
     time-averaged Cd in FP32, FP16, BF16 and FP64 storage with Smagorinsky
     Cs 0.1, each against FP64; and the examples/10 run (MRT without
     Smagorinsky) in the same four storages, each against its FP64 run and
@@ -399,8 +399,8 @@ def _batch_rate(n_steps, barrier, max_over_ranks):
     graph (the host rebuilds the geometry of the new radii afterwards, inside
     the timed region)."""
     import torch
-    from lbm_jax_autodiff_gb300.batch import Batch, config5_instances
-    inst, sph = config5_instances()
+    from lbm_jax_autodiff_gb300.batch import Batch, mixed_sphere_instances
+    inst, sph = mixed_sphere_instances()
     b = Batch(inst)
     b.set_spheres(sph)
     b.set_equilibrium()
@@ -703,10 +703,10 @@ def run_profile_case(spec):
     import torch
     parts = spec.split(":")
     if parts[0] == "batch":
-        from lbm_jax_autodiff_gb300.batch import Batch, config5_instances
+        from lbm_jax_autodiff_gb300.batch import Batch, mixed_sphere_instances
         count = int(parts[1]) if len(parts) > 1 else 16
         steps = int(parts[2]) if len(parts) > 2 else 8
-        inst, sph = config5_instances(count)
+        inst, sph = mixed_sphere_instances(count)
         b = Batch(inst)
         b.set_spheres(sph)
         b.set_equilibrium()

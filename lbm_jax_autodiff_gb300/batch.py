@@ -172,7 +172,7 @@ class Batch:
         return n.value
 
 
-def config5_instances(count=64, seed=0, n_alpha=(5.0, 10.0, 20.0), re=50.0):
+def mixed_sphere_instances(count=64, seed=0, n_alpha=(5.0, 10.0, 20.0), re=50.0):
     """The batched workload: grids uniform over {64x32x32, 96x48x48,
     128x64x64}, radius uniform in [4, 8] * (ny / 32) cells, modes split evenly
     over {halfway, bouzidi} x {hard, sigmoid-soft} with alpha from n_alpha,

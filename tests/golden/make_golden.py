@@ -53,7 +53,7 @@ def pins():
 
 
 def channel():
-    """Config 1: 64x21x8 BGK channel, parabolic inlet peak 0.05, tau 0.8, 3000 steps."""
+    """Channel: 64x21x8 BGK, parabolic inlet peak 0.05, tau 0.8, 3000 steps."""
     nx, ny, nz, n = 64, 21, 8, 3000
     prof = drivers.parabolic_inlet(ny, nz, 0.05)
     solid = drivers.channel_walls(nx, ny, nz)
@@ -77,7 +77,7 @@ def channel():
 
 
 def sphere(periodic=False):
-    """Config 2: 96x48x48 MRT, Bouzidi hard sphere r=0.5 world (6 cells) at
+    """Sphere: 96x48x48 MRT, Bouzidi hard sphere r=0.5 world (6 cells) at
     world (-2,0,0) = lattice (24,24,24), U 0.05, nu 0.006 (Re 100), free-slip
     sides (periodic_yz=False; with periodic=True the examples/10 periodic
     sides), pre-collision guard, 2000 steps, Cd every step of the last 30%."""
@@ -136,8 +136,8 @@ def modes():
         _save_json("modes_96x48x48.json", out)
 
 
-def config3():
-    """dCd/dr at the config-3 grid: 96x48x48, MRT, Bouzidi ray-sphere q(r),
+def sphere_grad_96x48x48():
+    """dCd/dr at 96x48x48, MRT, Bouzidi ray-sphere q(r),
     r = 0.5 world (6 cells) centred at cell (24, 24, 24) = world (-2, 0, 0),
     Re 100 (nu 0.006, tau 0.518); FP64 autograd through the oracle (the
     jax.grad stand-in) over a 100-step window, for the hard sphere and the
@@ -157,7 +157,7 @@ def config3():
         cd.backward()
         out[name] = {"cd": float(cd.detach()), "dcd_dr": float(r.grad), "seconds": time.time() - t0,
                      "porosity": kw["porosity_mode"], "sharpness": kw.get("sharpness")}
-        _save_json("config3_grad_96x48x48.json", out)
+        _save_json("sphere_grad_96x48x48.json", out)
 
 
 if __name__ == "__main__":

@@ -56,7 +56,7 @@ def test_aa_matches_ab(cuda, storage, collision, smag, guard, sph):
 
 
 def test_aa_channel_with_inlet_profile(cuda):
-    """The 64x21x8 channel of config 1 (solid walls, parabolic inlet, BGK)."""
+    """The 64x21x8 channel (solid walls, parabolic inlet, BGK)."""
     nx, ny, nz = 64, 21, 8
     prof = drivers.parabolic_inlet(ny, nz, 0.05)
     face = torch.stack([prof, torch.zeros_like(prof), torch.zeros_like(prof)]).contiguous().cuda()

@@ -2,11 +2,11 @@
 radii in [4, 8] * ny / 32 cells, modes split evenly, reproducible seed."""
 import numpy as np
 
-from lbm_jax_autodiff_gb300.batch import config5_instances
+from lbm_jax_autodiff_gb300.batch import mixed_sphere_instances
 
 
-def test_config5_draw():
-    inst, sph = config5_instances()
+def test_mixed_sphere_draw():
+    inst, sph = mixed_sphere_instances()
     assert len(inst) == 64 and len(sph) == 64
     grids = {(i["nx"], i["ny"], i["nz"]) for i in inst}
     assert grids <= {(64, 32, 32), (96, 48, 48), (128, 64, 64)} and len(grids) == 3
@@ -20,7 +20,7 @@ def test_config5_draw():
     modes = [(s["q_mode"], s["porosity"]) for s in sph]
     for m in [("halfway", "hard"), ("bouzidi", "hard"), ("halfway", "soft"), ("bouzidi", "soft")]:
         assert modes.count(m) == 16
-    inst2, sph2 = config5_instances()
+    inst2, sph2 = mixed_sphere_instances()
     assert inst == inst2 and sph == sph2
     cells = sum(i["nx"] * i["ny"] * i["nz"] for i in inst)
     assert 64 * 65536 <= cells <= 64 * 524288

@@ -1,6 +1,6 @@
 """Fused sm_103a step vs the CPU oracle on the same inputs.
 
-Bar (the benchmark spec): velocity field within 1e-5 absolute and Cd within 1e-4
+Bar: velocity field within 1e-5 absolute and Cd within 1e-4
 relative of the FP32 restatement; FP64 mode within 1e-11 of the FP64 oracle.
 
 An FP32 Cd sampled in a transient is itself uncertain at about 1e-4
@@ -119,7 +119,7 @@ def _sim(nx, ny, nz, tau, collision, storage="fp32", **kw):
 
 
 def test_channel_bgk_parabolic(cuda):
-    """Config-1 channel (64x21x8 BGK, tau 0.8, parabolic inlet) for 200 steps."""
+    """The 64x21x8 BGK channel (tau 0.8, parabolic inlet) for 200 steps."""
     nx, ny, nz = 64, 21, 8
     prof = drivers.parabolic_inlet(ny, nz, 0.05)
     solid = drivers.channel_walls(nx, ny, nz)

@@ -29,7 +29,7 @@ def _u(f):
     return torch.einsum("ixyz,ia->axyz", f, e) / rho
 
 
-def test_channel_config1_3000_steps(cuda):
+def test_channel_64x21x8_3000_steps(cuda):
     """64x21x8 BGK channel, parabolic inlet, tau 0.8, 3000 steps: whole u field
     within 1e-5 of the FP32 oracle; L2 error vs the parabola as the oracle."""
     from lbm_jax_autodiff_gb300 import Simulation
@@ -51,7 +51,7 @@ def test_channel_config1_3000_steps(cuda):
 
 @pytest.mark.parametrize("name,periodic", [("sphere_96x48x48_periodic", True),
                                            ("sphere_96x48x48", False)])
-def test_sphere_config2_2000_steps(cuda, name, periodic):
+def test_sphere_96x48x48_2000_steps(cuda, name, periodic):
     """96x48x48 MRT Bouzidi sphere, Re 100, 2000 steps, Cd sampled every step
     over the last 30% (examples/10 step order, pre-collision guard)."""
     from lbm_jax_autodiff_gb300 import Simulation
@@ -83,12 +83,12 @@ def test_sphere_config2_2000_steps(cuda, name, periodic):
         # unsteady within the first flow-through time (Cd swings between ~0
         # and ~12); two FP32 trajectories separate, so only the window
         # statistics are compared here and the field is checked on a short
-        # horizon in test_sphere_config2_freeslip_short_horizon
+        # horizon in test_sphere_96x48x48_freeslip_short_horizon
         assert abs(cd.mean() - d["cd_mean"]) <= d["cd_std"]
 
 
-def test_sphere_config2_freeslip_short_horizon(cuda):
-    """Free-slip config 2 for 300 steps: the whole u field within 1e-5 of the
+def test_sphere_96x48x48_freeslip_short_horizon(cuda):
+    """The free-slip 96x48x48 sphere for 300 steps: the whole u field within 1e-5 of the
     oracle before the unsteadiness amplifies rounding differences."""
     from lbm_jax_autodiff_gb300 import Simulation
     from oracle import ops

@@ -1,4 +1,4 @@
-"""Config 4 at its full length: the 256x128x128 sphere (D = 32 cells, Re 100,
+"""The 256x128x128 sphere at the full length of its Cd study (D = 32 cells, Re 100,
 MRT, Bouzidi on the dist^2 <= r^2 mask, Zou-He, periodic y/z, pre-collision
 guard), 28,000 steps, Cd sampled every 500 steps and averaged over the last
 30 % of the samples as examples/10_cd_convergence.py:88-106 does.

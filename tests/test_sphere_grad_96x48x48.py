@@ -1,6 +1,6 @@
-"""Shape gradient at the config-3 size and the reference's alpha sweep.
+"""Shape gradient of the 96x48x48 sphere and the reference's alpha sweep.
 
-Config 3: dCd/dr through 2000 MRT steps at 96x48x48 with Bouzidi ray-sphere
+dCd/dr through 2000 MRT steps at 96x48x48 with Bouzidi ray-sphere
 q(r), r = 0.5 world (6 cells) centred at cell (24, 24, 24), Re 100, for the
 hard sphere and the sigmoid-soft sphere (alpha 20):
   - FP32 result identical to the bit for segment lengths K = 50, 100, 200
@@ -10,8 +10,8 @@ hard sphere and the sigmoid-soft sphere (alpha 20):
     FP64 GPU forward, and within 1e-6 at dr = 1e-5 (the O(dr^2) error of the
     difference quotient shrinking);
   - on a 100-step window at the full grid, the FP64 adjoint against FP64
-    autograd through the oracle (tests/golden/config3_grad_96x48x48.json,
-    made by tests/golden/make_golden.py config3), to 1e-8.
+    autograd through the oracle (tests/golden/sphere_grad_96x48x48.json,
+    made by tests/golden/make_golden.py sphere_grad_96x48x48), to 1e-8.
 
 Alpha sweep: examples/12_sharpness_sensitivity.py:107-132 -- 96x48x48,
 Re 50, 2880 MRT steps, smooth sphere (sigmoid porosity, ray-sphere q),
@@ -83,7 +83,7 @@ def _fd(tau, center, sph, n, h, radius=0.5):
 
 
 @pytest.mark.parametrize("mode", sorted(MODES3))
-def test_config3_gradient_2000_steps(cuda, mode):
+def test_sphere_gradient_2000_steps(cuda, mode):
     sph = MODES3[mode]
     base = _grad("fp32", TAU3, CENTER3, sph, 2000, K=50)
     for K in (100, 200, 0):
@@ -99,8 +99,8 @@ def test_config3_gradient_2000_steps(cuda, mode):
 
 
 @pytest.mark.parametrize("mode", sorted(MODES3))
-def test_config3_grid_vs_oracle_autograd(cuda, mode):
-    with open(os.path.join(GOLDEN, "config3_grad_96x48x48.json")) as fh:
+def test_sphere_grad_vs_oracle_autograd(cuda, mode):
+    with open(os.path.join(GOLDEN, "sphere_grad_96x48x48.json")) as fh:
         gold = json.load(fh)
     ref = gold[mode]
     n = gold["steps"]
