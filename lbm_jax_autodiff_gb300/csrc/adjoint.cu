@@ -358,29 +358,24 @@ __device__ __forceinline__ long long dir_off(const AdjPairArgs<St>& P, int i) {
   const Grid& g = P.A.s.g;
   return (long long)(ex(i) * g.ny * g.nz + ey(i) * g.nz + ez(i));
 }
-template <class St>
+// ARITH (a template argument): formed from the state pointers and grid sizes
+// regardless of LBM_PAIR_PTR_ARITH -- the batched kernel's argument block
+// sits in shared memory, where a table entry costs a shared load per use.
+template <bool ARITH, class St>
 __device__ __forceinline__ const St* adj_pull(const AdjPairArgs<St>& P, int i) {
-#if LBM_PAIR_PTR_ARITH
-  return static_cast<const St*>(P.A.s.src) + (long long)i * P.A.s.g.n - dir_off(P, i);
-#else
+  if (ARITH || LBM_PAIR_PTR_ARITH)
+    return static_cast<const St*>(P.A.s.src) + (long long)i * P.A.s.g.n - dir_off(P, i);
   return P.pull[i];
-#endif
 }
-template <class St>
+template <bool ARITH, class St>
 __device__ __forceinline__ const float* adj_push(const AdjPairArgs<St>& P, int j) {
-#if LBM_PAIR_PTR_ARITH
-  return P.A.nu_in + (long long)j * P.A.s.g.n + dir_off(P, j);
-#else
+  if (ARITH || LBM_PAIR_PTR_ARITH) return P.A.nu_in + (long long)j * P.A.s.g.n + dir_off(P, j);
   return P.push[j];
-#endif
 }
-template <class St>
+template <bool ARITH, class St>
 __device__ __forceinline__ float* adj_out(const AdjPairArgs<St>& P, int i) {
-#if LBM_PAIR_PTR_ARITH
-  return P.A.nu_out + (long long)i * P.A.s.g.n;
-#else
+  if (ARITH || LBM_PAIR_PTR_ARITH) return P.A.nu_out + (long long)i * P.A.s.g.n;
   return P.out[i];
-#endif
 }
 
 #ifndef LBM_ADJ_PAIR_MINB
@@ -392,7 +387,7 @@ __device__ __forceinline__ float* adj_out(const AdjPairArgs<St>& P, int i) {
 // dJ/dp for a sigmoid sphere; lambda_k = C^T mu on the packed values; store
 // of nu_k.  Returns the pair's dJ/dr contribution
 // (nonzero only for a sigmoid sphere).
-template <class St, bool MRT, bool SOFT>
+template <class St, bool MRT, bool SOFT, bool ARITH = false>
 __device__ __forceinline__ double adj_pair_finish(const AdjPairArgs<St>& P, int idx, int x, int y,
                                                   int z, uint32_t t0, uint32_t t1, V2 mu[Q],
                                                   V2 f[Q]) {
@@ -447,7 +442,7 @@ __device__ __forceinline__ double adj_pair_finish(const AdjPairArgs<St>& P, int 
                     static_cast<V2*>(nullptr));
   // (x faces are listed pairs: no Zou-He transpose here)
 #pragma unroll
-  for (int i = 0; i < Q; ++i) *reinterpret_cast<float2*>(adj_out(P, i) + idx) = mu[i].v;
+  for (int i = 0; i < Q; ++i) *reinterpret_cast<float2*>(adj_out<ARITH>(P, i) + idx) = mu[i].v;
   return gr;
 }
 
@@ -477,7 +472,7 @@ __device__ __forceinline__ void adjoint_pair_list_part(const AdjPairArgs<St>& P,
 // One interior pair of interior block `iblock`: mu_k gathered from
 // nu_{k+1}, f_k pulled from S_{k-1}, then adj_pair_finish.  Returns the
 // pair's dJ/dr contribution.
-template <class St, bool MRT, bool SOFT>
+template <class St, bool MRT, bool SOFT, bool ARITH = false>
 __device__ __forceinline__ double adjoint_pair_interior(const AdjPairArgs<St>& P, int iblock) {
   using Pr = Pair<St>;
   const AdjArgs<float>& A = P.A;
@@ -504,7 +499,7 @@ __device__ __forceinline__ double adjoint_pair_interior(const AdjPairArgs<St>& P
 #pragma unroll
     for (int j = 0; j < Q; ++j) {
       const int b = ey(j) == 1 ? iyp : (ey(j) == -1 ? iym : idx);
-      const float* p = adj_push(P, j) + b;
+      const float* p = adj_push<ARITH>(P, j) + b;
       if (ez(j) == 0) mu[j] = V2(ldg_s(reinterpret_cast<const float2*>(p)));
       else if (ez(j) == 1) mu[j] = V2(ldg_s(p), ldg_s(p + 1 + zw1));
       else mu[j] = V2(ldg_s(p + zw0), ldg_s(p + 1));
@@ -525,23 +520,23 @@ __device__ __forceinline__ double adjoint_pair_interior(const AdjPairArgs<St>& P
 #pragma unroll
     for (int i = 0; i < Q; ++i) {
       const int b = ey(i) == 1 ? iym : (ey(i) == -1 ? iyp : idx);
-      const St* p = adj_pull(P, i) + b;
+      const St* p = adj_pull<ARITH>(P, i) + b;
       const V2 so(P.soff2[cls][i]);
       if (ez(i) == 0) f[i] = Pr::ld2(p, so);
       else if (ez(i) == 1) f[i] = Pr::ld2s(p + zw0, p + 1, so);
       else f[i] = Pr::ld2s(p, p + 1 + zw1, so);
     }
   }
-  return adj_pair_finish<St, MRT, SOFT>(P, idx, x, y, z, t0, t1, mu, f);
+  return adj_pair_finish<St, MRT, SOFT, ARITH>(P, idx, x, y, z, t0, t1, mu, f);
 }
 
 
 // Interior block `iblock`; a sigmoid sphere's dJ/dr partials go to the
 // per-cell slots gr_partials[iblock * 8 + warp] (256 cells per block, as the
 // blocks of k_adjoint).
-template <class St, bool MRT, bool SOFT>
+template <class St, bool MRT, bool SOFT, bool ARITH = false>
 __device__ __forceinline__ void adjoint_pair_interior_part(const AdjPairArgs<St>& P, int iblock) {
-  double gr = adjoint_pair_interior<St, MRT, SOFT>(P, iblock);
+  double gr = adjoint_pair_interior<St, MRT, SOFT, ARITH>(P, iblock);
   if (SOFT && (P.A.s.flags & SF_SOLID_SPHERE)) {
 #pragma unroll
     for (int o = 16; o > 0; o >>= 1) gr += __shfl_down_sync(0xffffffffu, gr, o);
@@ -782,6 +777,12 @@ __global__ void __launch_bounds__(256, LBM_ADJ_BATCH_MINB)
 #ifndef LBM_ADJ_PAIR_BATCH_MINB
 #define LBM_ADJ_PAIR_BATCH_MINB 4
 #endif
+// LBM_BATCH_PTR_ARITH 1: the batched pair adjoint forms its per-direction
+// pointers from the instance's state pointers (adj_pull<true>), 0: it
+// builds the tables in shared memory.
+#ifndef LBM_BATCH_PTR_ARITH
+#define LBM_BATCH_PTR_ARITH 1
+#endif
 
 template <bool MRT, bool SOFT>
 __global__ void __launch_bounds__(kAdjPairBlock, LBM_ADJ_PAIR_BATCH_MINB)
@@ -809,7 +810,7 @@ __global__ void __launch_bounds__(kAdjPairBlock, LBM_ADJ_PAIR_BATCH_MINB)
     A.dj_dfx = b.out + 4;
     A.gr_partials = b.gr_part;
     A.gq = b.gq;
-  } else if (threadIdx.x <= Q) {
+  } else if (!LBM_BATCH_PTR_ARITH && threadIdx.x <= Q) {
     // the per-direction tables, one direction per thread
     const int i = threadIdx.x - 1;
     const Grid& g = P.A.s.g;
@@ -829,7 +830,7 @@ __global__ void __launch_bounds__(kAdjPairBlock, LBM_ADJ_PAIR_BATCH_MINB)
     if (sb < nlist)
       adjoint_pair_list_part<float, MRT>(P, sb);
     else
-      adjoint_pair_interior_part<float, MRT, SOFT>(P, sb - nlist);
+      adjoint_pair_interior_part<float, MRT, SOFT, LBM_BATCH_PTR_ARITH != 0>(P, sb - nlist);
   }
 }
 

@@ -19,7 +19,10 @@ enum : int { SLOT_F0 = -1, SLOT_S0 = -2, SLOT_S1 = -3, SLOT_NU0 = -4, SLOT_NU1 =
 // Sub-blocks (one block's worth of cells each) that one block of a batched
 // launch walks after staging its instance's arguments once: map[b].y is the
 // first of them.
-constexpr int kBatchChunk = 4;
+#ifndef LBM_BATCH_CHUNK
+#define LBM_BATCH_CHUNK 4
+#endif
+constexpr int kBatchChunk = LBM_BATCH_CHUNK;
 
 // The same for the batched pair adjoint (sub-blocks of 128 pairs): one, so
 // the grid has the most blocks (measured 0.88 s per 400-step evaluation of
