@@ -379,9 +379,10 @@ void lbm_xla_momentum_exchange_vjp(void* stream, void** buffers, const char* opa
  * examples/10:69-106 (n_steps with the Cd sampled every sample_every steps),
  * lbm_xla_cd_and_grad the value_and_grad(simulate_cd) of examples/11:139-176.
  * The library keeps one solver handle per (device, params) for them, created
- * on first use and kept until exit; the sphere geometry (radius from the
- * operand) is rebuilt when it changes, which reads the radius back to the
- * host (a stream synchronisation).  The last result of each is an int32
+ * on first use; at most 8 are kept, the least recently used one that no call
+ * is using being destroyed for a new parameter set.  The sphere geometry
+ * (radius from the operand) is rebuilt when it changes, which reads the
+ * radius back to the host (a stream synchronisation).  The last result of each is an int32
  * status (lbm_status): on failure it is non-zero, the other results are
  * filled with NaN and the message goes to stderr. */
 typedef struct lbm_xla_fused_desc {

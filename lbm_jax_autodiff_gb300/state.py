@@ -64,7 +64,9 @@ def _handle(state, params):
     sim = _CACHE.get(key)
     if sim is None:
         if len(_CACHE) >= 8:
-            _CACHE.pop(next(iter(_CACHE))).close()
+            # dropped, not closed: an autograd graph may still hold it for its
+            # backward; it is destroyed with its last reference
+            _CACHE.pop(next(iter(_CACHE)))
         sim = Simulation(nx, ny, nz, float(params.tau),
                          collision="mrt" if int(params.collision_mode) == 1 else "bgk",
                          storage="fp64" if f.dtype == torch.float64 else "fp32",

@@ -127,3 +127,30 @@ def test_xla_fused_failure_sets_status_and_nan(cuda):
     _run_raw("cd_and_grad", [f0, r, cd, g, dq, status], _fused(nx, ny, nz, 0.4, n))
     assert int(status) == nat.LBM_ERR_ARG
     assert torch.isnan(cd).all() and torch.isnan(g).all() and torch.isnan(dq).all()
+
+
+def test_xla_fused_handles_beyond_the_cache_bound(cuda):
+    """Twelve parameter sets (more than the library keeps handles for) run in
+    turn and then again: every call matches its own solver handle, so evicted
+    handles are rebuilt, not reused."""
+    nx, ny, nz, n = 16, 8, 8, 10
+    sph = dict(kind="dist", q_mode="bouzidi", porosity="hard")
+    taus = [0.52 + 0.01 * k for k in range(12)]
+    ref = {}
+    for tau in taus:
+        sim = L.Simulation(nx, ny, nz, tau, collision="mrt", use_smagorinsky=True)
+        sim.set_sphere(0.5, **sph)
+        f0 = sim.equilibrium_state().contiguous()
+        sim.set_state(f0)
+        sim.run(n)
+        ref[tau] = (f0, sim.get_state())
+        sim.close()
+    r = torch.tensor([0.5], dtype=torch.float64, device="cuda")
+    smp = torch.zeros((1, 4), dtype=torch.float64, device="cuda")
+    status = torch.full((1,), -1, dtype=torch.int32, device="cuda")
+    for tau in taus + taus[:3]:
+        f0, f_ref = ref[tau]
+        f = torch.empty_like(f0)
+        _run_raw("run", [f0, r, f, smp, status], _fused(nx, ny, nz, tau, n, **sph))
+        assert int(status) == 0, tau
+        assert torch.equal(f, f_ref), tau
