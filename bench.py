@@ -265,7 +265,7 @@ def _state_api_rate(n_steps=200):
     import torch
     from lbm_jax_autodiff_gb300 import Simulation
     from lbm_jax_autodiff_gb300.geometry.primitives import create_sphere
-    from lbm_jax_autodiff_gb300.state import LBMParams, LBMState, simulate, step
+    from lbm_jax_autodiff_gb300.state import LBMParams, LBMState, clear_handles, simulate, step
     solid, q = create_sphere(NX, NY, NZ, (0.0, 0.0, 0.0), 0.5)
     solid = solid.to(torch.int32)
     sim = Simulation(NX, NY, NZ, TAU, collision="mrt", use_smagorinsky=True, smagorinsky_cs=CS,
@@ -296,6 +296,8 @@ def _state_api_rate(n_steps=200):
 
     t_sim = timed(lambda: simulate(state, params, n_steps))
     t_step = timed(loop)
+    clear_handles()                                # its device memory back for the next lines
+    torch.cuda.empty_cache()
     return {"steps": n_steps, "run_us_per_step": round(t_run, 2),
             "simulate_us_per_step": round(t_sim, 2), "step_loop_us_per_step": round(t_step, 2),
             "simulate_over_run": round(t_sim / t_run, 3), "step_loop_over_run": round(t_step / t_run, 3),

@@ -15,12 +15,12 @@ from .core.lattice import CS2, D3Q19_OPPOSITE, D3Q19_VELOCITIES, D3Q19_WEIGHTS
 from .core.streaming import stream
 from .batch import Batch
 from .solver import Simulation
-from .state import LBMParams, LBMState, simulate, step
+from .state import LBMParams, LBMState, clear_handles, simulate, step
 
 __all__ = [
     "D3Q19_VELOCITIES", "D3Q19_WEIGHTS", "D3Q19_OPPOSITE", "CS2",
     "equilibrium", "compute_density", "compute_velocity",
     "bgk", "mrt", "smagorinsky_tau", "stream", "zou_he_inlet", "zou_he_outlet",
     "momentum_exchange", "drag_coefficient", "projected_area",
-    "LBMState", "LBMParams", "step", "simulate", "Simulation", "Batch",
+    "LBMState", "LBMParams", "step", "simulate", "clear_handles", "Simulation", "Batch",
 ]

@@ -81,6 +81,13 @@ def _handle(state, params):
     return sim
 
 
+def clear_handles():
+    """Drop the solver handles step / simulate keep per parameter set; each is
+    destroyed, with its device memory, when its last reference goes (an
+    autograd graph awaiting its backward keeps its own)."""
+    _CACHE.clear()
+
+
 def _set_geometry(sim, solid, q):
     """set_mask unless solid and q are the tensors of the last call, unmodified.
     The handle keeps references to them, so their storage cannot be reused by

@@ -359,3 +359,5 @@ def test_state_calls_mixed_with_restarts(cuda):
     ref = L.simulate(L.LBMState(f=g, solid=st.solid, q=st.q), pr, 2)
     assert torch.equal(c.f, ref.f)
     assert torch.equal(c.f, L.simulate(st, pr, 7).f)
+    L.clear_handles()                                # a fresh handle gives the same f
+    assert torch.equal(c.f, L.simulate(st, pr, 7).f)
