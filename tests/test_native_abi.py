@@ -132,3 +132,23 @@ def test_ctypes_structs_match_the_library_layout(lib):
     assert L.lbm_struct_size(3) == ctypes.sizeof(jax_ffi.LBMXlaFusedDescC)
     assert L.lbm_struct_size(4) == ctypes.sizeof(nat.LBMAdamC)
     assert L.lbm_struct_size(99) == 0
+
+
+def test_jax_wrappers_build_without_jax(monkeypatch):
+    """The jax.ffi wrappers build (custom_vjp rules attached) against the
+    jax stand-in of tests/jaxlike.py; the GPU test runs them."""
+    import sys
+
+    import jaxlike
+    from lbm_jax_autodiff_gb300 import jax_ffi
+    jax, jnp = jaxlike.make()
+    monkeypatch.setitem(sys.modules, "jax", jax)
+    monkeypatch.setitem(sys.modules, "jax.numpy", jnp)
+    monkeypatch.setattr(jax_ffi, "_fns", None)
+    fns = jax_ffi._build()
+    for name in ("compute_density", "compute_velocity", "equilibrium", "bgk", "mrt",
+                 "smagorinsky_tau", "soft_bounce_back", "stream", "zou_he_inlet",
+                 "zou_he_outlet", "momentum_exchange"):
+        f = fns[name]
+        assert f.fwd is not None and f.bwd is not None, name
+    assert callable(fns["fused_run"]) and callable(fns["simulate_cd"])
