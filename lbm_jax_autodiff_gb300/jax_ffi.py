@@ -8,10 +8,10 @@ backend.  Each function mirrors the jax_lbm signature it replaces:
     equilibrium(rho, u)                 core/equilibrium.py:90
     compute_density(f)                  core/equilibrium.py:22
     compute_velocity(f, rho)            core/equilibrium.py:51
-    bgk(f, tau) / mrt(f, tau)           core/collision.py:46,103   (scalar tau)
+    bgk(f, tau) / mrt(f, tau)           core/collision.py:46,103   (scalar or per-cell tau)
     smagorinsky_tau(f, tau, cs)         core/collision.py:187
     stream(f, q, periodic_yz)           core/streaming.py:40
-    zou_he_inlet(f, velocity)           core/boundary.py:35        (scalar velocity)
+    zou_he_inlet(f, velocity, rho_target)  core/boundary.py:35     (uniform or face velocity)
     zou_he_outlet(f, rho_out)           core/boundary.py:127
     momentum_exchange(f_post, f_s, q)   core/forces.py:37
     soft_bounce_back(f, porosity)       geometry/smooth.py:118
@@ -181,6 +181,7 @@ def _build():
     equilibrium.defvjp(_eq_fwd, _eq_bwd)
 
     def _collide(kind):
+        # scalar tau: a static argument
         @functools.partial(jax.custom_vjp, nondiff_argnums=(1,))
         def fn(f, tau):
             nx, ny, nz = _dims(f)
@@ -197,10 +198,33 @@ def _build():
             return (gf,)
 
         fn.defvjp(fwd, bwd)
-        return fn
 
-    bgk = _collide("bgk")
-    mrt = _collide("mrt")
+        # per-cell tau (smagorinsky_tau's output, collision.py:46-100): an
+        # operand, differentiable
+        @jax.custom_vjp
+        def fn_field(f, tau):
+            nx, ny, nz = _dims(f)
+            return _call(kind, _sds(f.shape, f.dtype), f, tau,
+                         desc=descriptor(nx, ny, nz, _code(f), tau_field=1))
+
+        def fwd_field(f, tau):
+            return fn_field(f, tau), (f, tau)
+
+        def bwd_field(res, g):
+            f, tau = res
+            nx, ny, nz = _dims(f)
+            return tuple(_call(kind + "_vjp", (_sds(f.shape, f.dtype), _sds(tau.shape, f.dtype)),
+                               f, tau, g, desc=descriptor(nx, ny, nz, _code(f), tau_field=1)))
+
+        fn_field.defvjp(fwd_field, bwd_field)
+
+        def collide(f, tau):
+            return fn_field(f, tau) if getattr(tau, "ndim", 0) else fn(f, tau)
+
+        return collide, fn, fn_field
+
+    bgk, _bgk_scalar, _bgk_field = _collide("bgk")
+    mrt, _mrt_scalar, _mrt_field = _collide("mrt")
 
     @functools.partial(jax.custom_vjp, nondiff_argnums=(1, 2))
     def smagorinsky_tau(f, tau, cs=0.1):
@@ -253,22 +277,58 @@ def _build():
 
     stream.defvjp(_st_fwd, _st_bwd)
 
-    @functools.partial(jax.custom_vjp, nondiff_argnums=(1,))
-    def zou_he_inlet(f, velocity):
+    def _inlet_desc(f, velocity, rho_target, face):
         nx, ny, nz = _dims(f)
+        rt = rho_target is not None
+        return descriptor(nx, ny, nz, _code(f), u_face=int(face), has_rho_target=int(rt),
+                          u=(0.0, 0.0, 0.0) if face else tuple(float(c) for c in velocity),
+                          rho=float(rho_target) if rt else 1.0)
+
+    # uniform velocity: static arguments
+    @functools.partial(jax.custom_vjp, nondiff_argnums=(1, 2))
+    def _zi_uniform(f, velocity, rho_target):
         return _call("zou_he_inlet", _sds(f.shape, f.dtype), f,
-                     desc=descriptor(nx, ny, nz, _code(f), u=tuple(velocity)))
+                     desc=_inlet_desc(f, velocity, rho_target, False))
 
-    def _zi_fwd(f, velocity):
-        return zou_he_inlet(f, velocity), f
+    def _zi_fwd(f, velocity, rho_target):
+        return _zi_uniform(f, velocity, rho_target), f
 
-    def _zi_bwd(velocity, f, g):
+    def _zi_bwd(velocity, rho_target, f, g):
         nx, ny, nz = _dims(f)
         gf, _ = _call("zou_he_inlet_vjp", (_sds(f.shape, f.dtype), _sds((3, ny, nz), f.dtype)), f, g,
-                      desc=descriptor(nx, ny, nz, _code(f), u=tuple(velocity)))
+                      desc=_inlet_desc(f, velocity, rho_target, False))
         return (gf,)
 
-    zou_he_inlet.defvjp(_zi_fwd, _zi_bwd)
+    _zi_uniform.defvjp(_zi_fwd, _zi_bwd)
+
+    # a (3, ny, nz) velocity face (a parabolic profile, examples/01): an
+    # operand, differentiable
+    @functools.partial(jax.custom_vjp, nondiff_argnums=(2,))
+    def _zi_face(f, face, rho_target):
+        return _call("zou_he_inlet", _sds(f.shape, f.dtype), f, face,
+                     desc=_inlet_desc(f, None, rho_target, True))
+
+    def _zf_fwd(f, face, rho_target):
+        return _zi_face(f, face, rho_target), (f, face)
+
+    def _zf_bwd(rho_target, res, g):
+        f, face = res
+        return tuple(_call("zou_he_inlet_vjp", (_sds(f.shape, f.dtype), _sds(face.shape, f.dtype)),
+                           f, face, g, desc=_inlet_desc(f, None, rho_target, True)))
+
+    _zi_face.defvjp(_zf_fwd, _zf_bwd)
+
+    def zou_he_inlet(f, velocity, rho_target=None):
+        """velocity: three components, each a scalar or a (ny, nz) face, or a
+        (3, ny, nz) array (boundary.py:35-124)."""
+        if getattr(velocity, "ndim", 0) == 3:
+            return _zi_face(f, velocity, rho_target)
+        if any(getattr(c, "ndim", 0) for c in velocity):
+            ny, nz = int(f.shape[2]), int(f.shape[3])
+            face = jnp.stack([jnp.broadcast_to(jnp.asarray(c, f.dtype), (ny, nz))
+                              for c in velocity])
+            return _zi_face(f, face, rho_target)
+        return _zi_uniform(f, tuple(float(c) for c in velocity), rho_target)
 
     @functools.partial(jax.custom_vjp, nondiff_argnums=(1,))
     def zou_he_outlet(f, rho_out=1.0):
@@ -344,7 +404,10 @@ def _build():
                 equilibrium=equilibrium, bgk=bgk, mrt=mrt, smagorinsky_tau=smagorinsky_tau,
                 soft_bounce_back=soft_bounce_back, stream=stream, zou_he_inlet=zou_he_inlet,
                 zou_he_outlet=zou_he_outlet, momentum_exchange=momentum_exchange,
-                fused_run=fused_run, simulate_cd=simulate_cd)
+                fused_run=fused_run, simulate_cd=simulate_cd,
+                _bgk_scalar=_bgk_scalar, _mrt_scalar=_mrt_scalar, _bgk_field=_bgk_field,
+                _mrt_field=_mrt_field, _zi_uniform=_zi_uniform,
+                _zi_face=_zi_face)
 
 
 _fns = None

@@ -92,6 +92,8 @@ def make():
     jnp.float32, jnp.float64, jnp.int32 = torch.float32, torch.float64, torch.int32
     jnp.asarray = _asarray
     jnp.zeros_like = torch.zeros_like
+    jnp.stack = lambda xs: torch.stack(list(xs)).contiguous()
+    jnp.broadcast_to = torch.broadcast_to
     jax = types.ModuleType("jax")
     jax.numpy = jnp
     jax.ffi = _Ffi()

@@ -68,15 +68,34 @@ def test_per_op_wrappers_match_the_torch_dropins(jf):
     _check(jax, jax_ffi.compute_density, L.compute_density, (f,), (0,))
     _check(jax, jax_ffi.compute_velocity, L.compute_velocity, (f, rho), (0, 1))
     _check(jax, jax_ffi.equilibrium, L.equilibrium, (rho, u), (0, 1))
-    _check(jax, jax_ffi.mrt, lambda a, t: L.mrt(a, t), (f, 0.6), (0,))
-    _check(jax, jax_ffi.bgk, lambda a, t: L.bgk(a, t), (f, 0.6), (0,))
+    jax_ffi.mrt                                      # builds the wrappers
+    fns = jax_ffi._fns
+    _check(jax, fns["_mrt_scalar"], lambda a, t: L.mrt(a, t), (f, 0.6), (0,))
+    _check(jax, fns["_bgk_scalar"], lambda a, t: L.bgk(a, t), (f, 0.6), (0,))
+    assert torch.equal(jax_ffi.mrt(f, 0.6), L.mrt(f, 0.6))
     _check(jax, jax_ffi.smagorinsky_tau, lambda a, t, c: L.smagorinsky_tau(a, t, c),
            (f, 0.55, 0.1), (0,))
     _check(jax, jax_ffi.soft_bounce_back, soft_bounce_back, (f, por), (0, 1))
     _check(jax, jax_ffi.stream, lambda a, b, p: L.stream(a, b, p), (f, q, True), (0, 1))
     _check(jax, jax_ffi.stream, lambda a, b, p: L.stream(a, b, p), (f, q, False), (0, 1))
-    _check(jax, jax_ffi.zou_he_inlet, lambda a, v: L.zou_he_inlet(a, v), (f, (0.05, 0.0, 0.01)),
-           (0,))
+    _check(jax, fns["_zi_uniform"], lambda a, v, r: L.zou_he_inlet(a, v, r),
+           (f, (0.05, 0.0, 0.01), None), (0,))
+    _check(jax, fns["_zi_uniform"], lambda a, v, r: L.zou_he_inlet(a, v, r),
+           (f, (0.05, 0.0, 0.0), 1.02), (0,))
+    prof = drivers.parabolic_inlet(f.shape[2], f.shape[3], 0.05, f.dtype).cuda()
+    face = torch.stack([prof, 0.1 * prof, torch.zeros_like(prof)]).contiguous()
+    _check(jax, fns["_zi_face"], lambda a, fc, r: L.zou_he_inlet(a, (fc[0], fc[1], fc[2]), r),
+           (f, face, None), (0, 1))
+    # the public dispatchers pick those forms
+    assert torch.equal(jax_ffi.zou_he_inlet(f, (prof, 0.1 * prof, 0.0)),
+                       L.zou_he_inlet(f, (prof, 0.1 * prof, 0.0)))
+    assert torch.equal(jax_ffi.zou_he_inlet(f, (0.05, 0.0, 0.0), 1.02),
+                       L.zou_he_inlet(f, (0.05, 0.0, 0.0), 1.02))
+    tau_field = L.smagorinsky_tau(f, 0.55, 0.1)
+    for kind in ("mrt", "bgk"):
+        _check(jax, fns["_%s_field" % kind], lambda a, t: getattr(L, kind)(a, t),
+               (f, tau_field), (0, 1))
+        assert torch.equal(getattr(jax_ffi, kind)(f, tau_field), getattr(L, kind)(f, tau_field))
     _check(jax, jax_ffi.zou_he_outlet, lambda a, r: L.zou_he_outlet(a, r), (f, 1.01), (0,))
     fs = _f(seed=4)
     _check(jax, jax_ffi.momentum_exchange, L.momentum_exchange, (f, fs, q), (0, 1), tol=1e-12)

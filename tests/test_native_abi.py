@@ -146,9 +146,11 @@ def test_jax_wrappers_build_without_jax(monkeypatch):
     monkeypatch.setitem(sys.modules, "jax.numpy", jnp)
     monkeypatch.setattr(jax_ffi, "_fns", None)
     fns = jax_ffi._build()
-    for name in ("compute_density", "compute_velocity", "equilibrium", "bgk", "mrt",
-                 "smagorinsky_tau", "soft_bounce_back", "stream", "zou_he_inlet",
-                 "zou_he_outlet", "momentum_exchange"):
+    for name in ("compute_density", "compute_velocity", "equilibrium", "smagorinsky_tau",
+                 "soft_bounce_back", "stream", "zou_he_outlet", "momentum_exchange",
+                 "_bgk_scalar", "_mrt_scalar", "_bgk_field", "_mrt_field", "_zi_uniform",
+                 "_zi_face"):
         f = fns[name]
         assert f.fwd is not None and f.bwd is not None, name
-    assert callable(fns["fused_run"]) and callable(fns["simulate_cd"])
+    for name in ("bgk", "mrt", "zou_he_inlet", "fused_run", "simulate_cd"):
+        assert callable(fns[name]), name
