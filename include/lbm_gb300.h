@@ -189,6 +189,12 @@ int lbm_cd_and_grad(lbm_sim* sim, int n_steps, int checkpoint_every, double* cd_
 int lbm_vjp_run(lbm_sim* sim, int n_steps, int checkpoint_every, const void* g_f_final,
                 void* g_f0, void* g_q, void* stream);
 
+/* The checkpoint plan the automatic setting (checkpoint_every <= 0) makes
+ * for n_steps when max_states population states fit: the longest segment K
+ * with ceil(n_steps / K) - 1 + K <= max_states (n_steps - K steps are then
+ * recomputed).  LBM_ERR_NOMEM when no K fits.  No GPU call. */
+int lbm_plan_checkpoints(int n_steps, long long max_states, int* segment_steps);
+
 /* Plan of the last lbm_cd_and_grad: segment length, recomputed steps and
  * the bytes of the population workspace (checkpoints + stash). */
 int lbm_get_adjoint_plan(lbm_sim* sim, int* segment_steps, int* recomputed_steps,

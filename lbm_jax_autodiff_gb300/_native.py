@@ -120,6 +120,7 @@ SIGNATURES = {
     "lbm_get_link_count": [_vp, ctypes.POINTER(_i), ctypes.POINTER(_i)],
     "lbm_get_guard_resets": [_vp, ctypes.POINTER(ctypes.c_ulonglong), _vp],
     "lbm_get_steps": [_vp, ctypes.POINTER(_ll)],
+    "lbm_plan_checkpoints": [_i, ctypes.c_longlong, ctypes.POINTER(_i)],
     "lbm_get_adjoint_plan": [_vp, ctypes.POINTER(_i), ctypes.POINTER(_i),
                              ctypes.POINTER(ctypes.c_ulonglong)],
     "lbm_release_workspace": [_vp],

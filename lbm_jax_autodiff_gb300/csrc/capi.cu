@@ -953,6 +953,12 @@ int lbm_get_guard_resets(lbm_sim* s, unsigned long long* count_host, void* strea
   return cuda_check(cudaStreamSynchronize(st), "sync");
 }
 
+int lbm_plan_checkpoints(int n_steps, long long max_states, int* segment_steps) {
+  if (n_steps < 1 || !segment_steps)
+    return set_error(LBM_ERR_ARG, "lbm_plan_checkpoints: n_steps < 1 or null segment_steps");
+  return plan_segment(n_steps, max_states, 1, segment_steps);
+}
+
 int lbm_get_adjoint_plan(lbm_sim* s, int* segment_steps, int* recomputed_steps,
                          unsigned long long* workspace_bytes) {
   if (!s || !segment_steps || !recomputed_steps || !workspace_bytes)

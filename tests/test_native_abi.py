@@ -154,3 +154,28 @@ def test_jax_wrappers_build_without_jax(monkeypatch):
         assert f.fwd is not None and f.bwd is not None, name
     for name in ("bgk", "mrt", "zou_he_inlet", "fused_run", "simulate_cd"):
         assert callable(fns[name]), name
+
+
+def test_checkpoint_plan_is_the_longest_segment_that_fits(lib):
+    """lbm_plan_checkpoints (the automatic plan's search, host code) against
+    a brute-force search over every segment length: the longest K with
+    ceil(N/K) - 1 + K <= M, and LBM_ERR_NOMEM exactly when none fits."""
+    import ctypes
+
+    from lbm_jax_autodiff_gb300 import _native as nat
+    L = nat.load()
+
+    def states(n, k):
+        return (n + k - 1) // k - 1 + k
+
+    k = ctypes.c_int()
+    for n in list(range(1, 120)) + [2000, 2880, 28000]:
+        lo = min(states(n, j) for j in range(1, n + 1))
+        for m in sorted({0, 1, 2, lo - 1, lo, lo + 1, n // 2, n - 1, n, n + 5, 10 ** 9}):
+            rc = L.lbm_plan_checkpoints(n, m, ctypes.byref(k))
+            fit = [j for j in range(1, n + 1) if states(n, j) <= m]
+            if fit:
+                assert rc == nat.LBM_OK and k.value == max(fit), (n, m, k.value)
+            else:
+                assert rc == nat.LBM_ERR_NOMEM, (n, m)
+    assert L.lbm_plan_checkpoints(0, 10, ctypes.byref(k)) == nat.LBM_ERR_ARG
