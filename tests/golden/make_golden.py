@@ -115,6 +115,40 @@ def sphere_periodic():
     sphere(periodic=True)
 
 
+def sphere_freeslip_fp64():
+    """The free-slip 96x48x48 sphere of sphere() in FP64 (the oracle's FP64
+    constants, those of the fused solver's FP64 storage mode): Cd every 100
+    steps over the 2000 steps and u at a few fixed cells at the end."""
+    dt = torch.float64
+    c = ops.consts_for(dt)
+    nx, ny, nz, n, every = 96, 48, 48, 2000, 100
+    U, nu = 0.05, 0.006
+    tau = 3 * nu + 0.5
+    center = (-2.0, 0.0, 0.0)
+    solid, q = geometry.create_sphere(nx, ny, nz, center, 0.5, dt)
+    f = drivers.initial_state(nx, ny, nz, U, dt, c)
+    cfg = drivers.StepConfig(tau=tau, inlet=(U, 0.0, 0.0), collision="mrt",
+                             periodic_yz=False, guard="pre")
+    area = max(ops.projected_area(solid), 1.0)
+    cds = []
+
+    def cb(k, fs, fp):
+        if k % every == 0:
+            cds.append(float(drivers.cd_from(fp, fs, q, U, area)[0]))
+
+    t0 = time.time()
+    with torch.no_grad():
+        f, _, _ = drivers.run(f, q, cfg, n, solid=solid, f_ref=f, sample_every=1, on_sample=cb,
+                              consts=c)
+    u = ops.compute_velocity(f, ops.compute_density(f))
+    probes = [(40, 24, 24), (30, 10, 40), (60, 24, 5), (90, 40, 40), (10, 0, 0)]
+    _save_json("sphere_96x48x48_freeslip_fp64.json", {
+        "grid": [nx, ny, nz], "steps": n, "tau": tau, "U": U, "center": center, "radius": 0.5,
+        "sample_every": every, "cd": cds, "probes": probes,
+        "u_probes": [[float(u[a, x, y, z]) for a in range(3)] for x, y, z in probes],
+        "seconds": time.time() - t0})
+
+
 def modes():
     """Four-mode base Cd, 96x48x48 MRT, Re 50, 2000 steps (examples/11:56-165);
     published (A100): halfway_hard 1.85, bouzidi_hard 1.77, halfway_soft 0.43,

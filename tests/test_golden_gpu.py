@@ -110,6 +110,33 @@ def test_sphere_96x48x48_freeslip_short_horizon(cuda):
     assert (u_g - u_o).abs().max().item() <= 1e-5
 
 
+def test_sphere_96x48x48_freeslip_fp64_2000_steps(cuda):
+    """The free-slip 96x48x48 sphere as written (clamped y / z edges) in FP64
+    storage against the FP64 oracle (sphere_96x48x48_freeslip_fp64.json), Cd
+    every 100 steps.  Measured: the two FP64 trajectories agree to ~5e-14
+    through step 400 and 4e-11 at step 500; from there the difference grows
+    about 5000-fold per 100 steps (the flow is chaotic) and reaches O(1) by
+    step 800.  So Cd is held to 1e-12 through step 400 and 1e-9 at step 500;
+    later samples, in any arithmetic, are comparable only as window
+    statistics (test_sphere_96x48x48_2000_steps)."""
+    from lbm_jax_autodiff_gb300 import Simulation
+    from oracle import ops
+    d = _load("sphere_96x48x48_freeslip_fp64")
+    nx, ny, nz = d["grid"]
+    dt = torch.float64
+    sim = Simulation(nx, ny, nz, d["tau"], collision="mrt", storage="fp64", guard="pre",
+                     periodic_yz=False, inlet_velocity=(d["U"], 0.0, 0.0))
+    sim.set_sphere(0.5, center=tuple(d["center"]), kind="dist", q_mode="bouzidi", porosity="hard")
+    sim.set_state(drivers.initial_state(nx, ny, nz, d["U"], dt, ops.consts_for(dt)).cuda())
+    every = d["sample_every"]
+    cd = sim.run(5 * every, sample_every=every)[:, 3].cpu().tolist()
+    rel = [abs(a - b) / abs(b) for a, b in zip(cd, d["cd"])]
+    print("rel Cd per 100 steps:", ["%.1e" % r for r in rel])
+    assert max(rel[:4]) <= 1e-12, rel
+    assert rel[4] <= 1e-9, rel
+    sim.close()
+
+
 def test_four_modes_base_cd(cuda):
     """Four-mode base Cd at r = 0.5 (examples/11, 96x48x48, MRT, Re 50, 2000
     steps): oracle fixture within 1e-3, published A100 values within 3%."""
