@@ -12,8 +12,9 @@
  *  - Populations use the reference layout [19][nx][ny][nz] (z fastest); fields
  *    [nx][ny][nz]; velocity [3][nx][ny][nz]; inlet faces [3][ny][nz].
  *  - dtype arguments take lbm_dtype; per-op kernels support LBM_F32/LBM_F64.
- *  - Every function returns an lbm_status; LBM_OK = 0.  lbm_last_error() gives
- *    a message for the last failure on the calling thread.
+ *  - Every function returning int returns an lbm_status; LBM_OK = 0.
+ *    lbm_last_error() gives a message for the last failure on the calling
+ *    thread.  (The XLA targets return nothing; see their section.)
  *  - `stream` is a cudaStream_t (NULL = legacy default stream).  Calls are
  *    asynchronous with respect to the host unless stated otherwise.
  *  - Outputs are distinct from inputs (the reference functions are pure).
