@@ -65,3 +65,15 @@ def test_reference_arm_runs_on_rank_zero_only(monkeypatch):
     class A:
         steps, warmup = 1, 0
     assert bench.run_reference(A()) == 0      # returns at once, no oracle work
+
+
+def test_both_arms_print_the_same_config():
+    """The reference arm and this arm build their config from one function,
+    so the two JSON lines name the same workload at every world size."""
+    import inspect
+
+    import bench
+    for ws in (1, 2, 8):
+        assert bench.bench_config(ws) == bench.bench_config(ws)
+    for arm in (bench.run_reference, bench.run_ours):
+        assert '"config": bench_config(ws)' in inspect.getsource(arm), arm.__name__
